@@ -1,0 +1,318 @@
+"""Benchmark: reference-order two-watched-literal BCP propagations/s on GB300.
+
+Workload (the BCP microbenchmark configuration): seeded uniform random 3-SAT,
+n = 1,000,000 variables, m = 4,200,000 clauses (int32 signed-literal CSR arena);
+4096 independent seeded partial trails per step, each assigning a uniformly
+random 1-5% of the variables with random polarity at decision level 1.  One
+step = one pass of the BCP kernel over all 4096 trails (every trail literal
+assigned, then propagated in trail order depth-first until the first
+conflict, as the reference applies assumptions).  Outputs per trail: implied
+literals in order, reason clauses, conflict flag / clause, stop index.
+
+  value   propagations/s with inputs resident in HBM (CUDA events on the
+          launch stream, K back-to-back launches)
+  e2e     propagations/s through gpsat_bcp_run_host: pinned host trails in,
+          results out, copies inside the timed region
+  roofline  algorithmic bytes per launch (4*watch entries + 4*clause
+          literals + 1*assignment lookups + 9*implications + 5*trail
+          literals, counted by the kernel) / average launch time, against the
+          measured HBM copy bandwidth
+  cpu_baseline  the oracle's C restatement of the reference BCP (same
+          semantics and outputs) on the host cores, on a bounded sample
+
+`--impl reference` times the reference-semantics CPU path alone.  Under
+torchrun each rank runs its own 4096 trails (weak scaling; trails never
+exchange data) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BCP props/s"
+UNIT = "props/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpsat", choices=["gpsat", "reference"])
+    ap.add_argument("--n-vars", type=int, default=1_000_000)
+    ap.add_argument("--ratio", type=float, default=4.2)
+    ap.add_argument("--trails", type=int, default=4096)
+    ap.add_argument("--impl-cap", type=int, default=4096)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-trails", type=int, default=1024)
+    return ap.parse_args()
+
+
+def workload(args, rank):
+    import gpupsat_gb300 as g
+    n = args.n_vars
+    m = int(round(args.ratio * n))
+    lits, off = g.gen_random_ksat(2024, n, m, 3)
+    tl, to = g.gen_trails(7 + 1000 * rank, n, args.trails, 0.01, 0.05)
+    return n, m, lits, off, tl, to
+
+
+def config(args, n, m):
+    return {"workload": "BCP microbenchmark: random 3-SAT, partial trails",
+            "n_vars": n, "n_clauses": m, "n_trails": args.trails, "trail_fraction": [0.01, 0.05],
+            "literal_arena": "int32 CSR", "l2": "inputs larger than L2 (formula 0.3 GB, trails 0.5 GB, "
+                                               "per-trail state > 30 GB); no flush needed",
+            "semantics": "reference order (bit-exact reasons and conflict clause)"}
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in self.rows:
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def traffic_per_launch(n, trails):
+    """DRAM bytes per launch from the committed ncu summary, scaled by trail count."""
+    p = ROOT / "profiles" / "bcp_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    if d.get("n_vars") != n:
+        return None
+    return d["dram_bytes_per_trail"] * trails
+
+
+def alg_bytes(cnt):
+    W, L, A, I, T = (cnt[:, i].sum(dtype=np.float64) for i in range(1, 6))
+    return 4 * W + 4 * L + A + 9 * I + 5 * T
+
+
+def cpu_baseline(lits, off, n, tl, to, ntrails, threads):
+    import oracle
+    o = oracle.BCPOracle(lits, off, n)
+    T = min(ntrails, len(to) - 1)
+    sub_to = to[:T + 1].copy()
+    sub_tl = tl[:sub_to[-1]]
+    t0 = time.perf_counter()
+    r = o.run(sub_tl, sub_to, impl_cap=4096, threads=threads)
+    dt = time.perf_counter() - t0
+    props = int(r["counters"][:, 0].sum())
+    return props / dt, props, dt, T
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n, m, lits, off, tl, to = workload(args, 0)
+    threads = os.cpu_count() or 1
+    vals = []
+    per_step = max(64, min(args.cpu_trails, args.trails))
+    for s in range(args.warmup + args.steps):
+        # each step: a bounded sample of the same workload (trails rotate per step)
+        b = (s * per_step) % max(1, args.trails - per_step + 1)
+        sub_to = to[b:b + per_step + 1] - to[b]
+        sub_tl = tl[to[b]:to[b + per_step]]
+        v, props, dt, T = cpu_baseline(lits, off, n, sub_tl, sub_to, per_step, threads)
+        if s >= args.warmup:
+            vals.append((props, dt))
+    props = sum(p for p, _ in vals)
+    dt = sum(d for _, d in vals)
+    value = props / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / len(vals),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
+            "config": config(args, n, m),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} trails per step of the same workload; the reference's own "
+                                       f"BCP cannot hold n=1e6 (100k-node watch pool, O(n) per assignment), so "
+                                       f"its C restatement (oracle/bcp_ref.c, bit-exact with it) is timed"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import gpupsat_gb300 as g
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    n, m, lits, off, tl, to = workload(args, rank)
+    T = args.trails
+    cap = args.impl_cap
+    f = g.Formula(lits, off, n)
+    b = g.BCPBatch(f, impl_cap=cap)
+    d_tl = torch.from_numpy(tl).to(dev)
+    d_to = torch.from_numpy(to).to(dev)
+    out = dict(status=torch.empty(T, dtype=torch.int32, device=dev),
+               conflict=torch.empty(T, dtype=torch.int32, device=dev),
+               stop=torch.empty(T, dtype=torch.int32, device=dev),
+               n_impl=torch.empty(T, dtype=torch.int64, device=dev),
+               impl_lit=torch.empty(T, cap, dtype=torch.int32, device=dev),
+               impl_reason=torch.empty(T, cap, dtype=torch.int32, device=dev),
+               counters=torch.empty(T, 6, dtype=torch.int64, device=dev))
+    stream = torch.cuda.Stream(device=dev)
+    for _ in range(args.warmup):
+        b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
+    stream.synchronize()
+    cnt = out["counters"].cpu().numpy()
+    props_step = int(cnt[:, 0].sum())
+    bytes_step = alg_bytes(cnt)
+
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
+        evs[i + 1].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launch_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    elapsed = sum(launch_ms) / 1000.0
+    cnt2 = out["counters"].cpu().numpy()
+    assert int(cnt2[:, 0].sum()) == props_step, "propagation count changed between steps"
+    if dist:
+        t = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        pt = torch.tensor([props_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(pt)
+        props_all = float(pt.item())
+    else:
+        props_all = float(props_step)
+    value = props_all * args.steps / elapsed
+
+    # end to end through the host entry point (pinned buffers)
+    e2e = None
+    if not args.no_e2e:
+        p_tl = torch.from_numpy(tl).pin_memory().numpy()
+        p_to = torch.from_numpy(to).pin_memory().numpy()
+        h = b.run_host(p_tl, p_to)  # warm the staging buffers
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            h = b.run_host(p_tl, p_to)
+        e2e_s = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        maxn = int(h["n_impl"].max())
+        d2h = T * (4 * 3 + 8 + 8 * 6) + 2 * 4 * T * (maxn if maxn * 4 < cap * 2 else cap)
+        e2e = {"value": props_all * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(tl.nbytes + to.nbytes), "d2h_bytes_per_step": int(d2h)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_src = peaks()
+    avg_launch_s = elapsed / args.steps
+    achieved = bytes_step / avg_launch_s / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic_per_launch(n, T), "peak_source": peak_src,
+            "alg_bytes_per_launch": bytes_step, "kernel": "gpsat::bcp::bcp_kernel"}
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, props, dt, Tc = cpu_baseline(lits, off, n, tl, to, args.cpu_trails, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {Tc} of the {T} trails ({props} propagations, {dt:.1f} s); oracle/bcp_ref.c, "
+                         f"the reference's BCP semantics restated (bit-exact with it)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
+            "config": config(args, n, m), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": args.steps,
+            "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item())}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

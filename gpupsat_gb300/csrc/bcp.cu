@@ -1,0 +1,966 @@
+// Two-watched-literal BCP over a batch of partial trails, in the reference's
+// own processing order (bit-exact implied literals, reasons and conflict
+// clause), on sm_103a.
+//
+// Reference behaviour (paths inside the reference project, src/):
+//   trail application   SATSolver/VariablesStateHandler.cu:35-59 then
+//                       ConflictAnalysis/ConflictAnalyzerWithWatchedLits.cu:56-73
+//   new_decision        BCPStrategy/WatchedClausesList.cu:46-101 (snapshot of the
+//                       var's list, then depth-first over new implications)
+//   process_clause      BCPStrategy/WatchedClausesList.cu:103-221
+//   handle_implication  BCPStrategy/WatchedClausesList.cu:253-282
+//   block / switch      BCPStrategy/ClauseListStructure.cu:73-92, 150-164
+//
+// Layout (HBM):
+//   formula (shared by all trails, read-only)
+//     lits[]   internal literals, CSR by clause
+//     w0off[]  per-var offsets into w0ent
+//     w0ent[]  int4 {clause, lit offset, length, (w1<<16)|w2} per initial watch,
+//              each var's entries in the reference's initial list order
+//   per trail slot (one warp owns one slot; slots are reused across trails)
+//     asg[n]    uint8  (epoch<<1)|sign   trail + pending implications
+//     cst[m]    uint32 (epoch<<24)|(blocked<<22)|(w1<<11)|w2   clauses touched
+//     dh[n]     uint32 (epoch<<24)|arena index   head of clauses add_first'ed to a var
+//     arena[]   int4 {clause, lit offset, length, next}
+//     stack[]   int2 depth-first frames (intervals of the implication list)
+//   A slot's epoch (1..127) advances per trail, so nothing is cleared between
+//   trails; the slot is wiped once every 127 trails.
+//
+// Current list of var v = clauses add_first'ed to v (newest first) followed by
+// v's initial list, keeping entries whose clause still watches v and is not
+// blocked.  A clause never comes back to a var it left (watches only leave
+// false literals and nothing is unassigned within one BCP), so that is the
+// reference's linked list exactly.
+//
+// Execution: one warp per trail.  Each round gathers up to 32 upcoming watch
+// entries -- the rest of the current scan and, while the current scan is a
+// trail scan that has implied nothing, the entries of the following trail
+// scans -- evaluates all of them at once against the current state, then
+// commits them in reference order, stopping before the first entry whose
+// evaluation an earlier entry of the round may have changed (same clause, or
+// a scan whose list an earlier switch extended) and right after the first
+// implication or conflict.  What is not committed is evaluated again next
+// round, so the result is the sequential one.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+
+#include "internal.h"
+
+namespace gpsat {
+namespace bcp {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int WARPS = 4;          // warps per block
+constexpr int KREG = 8;           // clause literals evaluated from registers
+constexpr uint32_t EPMAX = 127;   // epochs per slot before a wipe
+constexpr int MAXLEN = 2048;      // clause length limit (11-bit watch indices)
+constexpr int64_t MAX_ITERS = int64_t(1) << 26;  // per-trail loop iterations before GPSAT_BCP_BUDGET
+
+enum : int { A_NONE = 0, A_SW1 = 1, A_SW2 = 2, A_BLOCK = 3, A_IMPLY = 4, A_CONFLICT = 5 };
+
+struct Dev {
+    int32_t n_vars;
+    int32_t n_clauses;
+    const int32_t *__restrict__ lits;
+    const uint32_t *__restrict__ w0off;
+    const int4 *__restrict__ w0ent;
+    uint8_t *asg;
+    uint32_t *cst;
+    uint32_t *dh;
+    int4 *arena;
+    int2 *stack;
+    uint32_t *epoch;
+    unsigned int *next_trail;
+    int64_t n_pad, m_pad, arena_cap, impl_cap;
+    int32_t n_slots;
+    const int32_t *__restrict__ trail;
+    const int64_t *__restrict__ toff;
+    int32_t n_trails;
+    int32_t *status, *conflict, *stop;
+    int64_t *nimpl;
+    int32_t *ilit, *ireason;
+    int64_t *counters;
+};
+
+struct WarpSmem {
+    int4 ent[32];
+    int32_t dp_after[32];
+    int32_t sc_var[33];
+    int32_t sc_begin[33];
+    int32_t sc_end[33];
+    uint32_t sc_wk[33];
+    uint32_t sc_wend[33];
+};
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned lanemask_gt()
+{
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_gt;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned range_mask(int b, int e)
+{
+    unsigned hi = e >= 32 ? FULL : ((1u << e) - 1u);
+    unsigned lo = b >= 32 ? FULL : ((1u << b) - 1u);
+    return hi & ~lo;
+}
+template <class T>
+__device__ __forceinline__ T warp_sum(T x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    return x;
+}
+__device__ __forceinline__ int32_t dimacs_of(int32_t l) { return (l & 1) ? (l >> 1) + 1 : -((l >> 1) + 1); }
+
+// consistency of literal l given its var's asg byte: unassigned in this epoch or true
+__device__ __forceinline__ bool cons_of(uint8_t a, int32_t l, uint32_t e)
+{
+    return ((uint32_t)(a >> 1) != e) || ((a & 1) == (l & 1));
+}
+
+struct Eval {
+    int act;
+    int nw1, nw2;       // new watch indices (switch)
+    int32_t t1, t2;     // switch target vars
+    uint32_t dh1, dh2;  // their list heads as loaded
+    int32_t unit;       // unit literal (imply)
+    int acnt;           // assignment lookups as the reference counts them
+};
+
+// process_clause of the reference for one clause with watch indices w1, w2.
+__device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const uint32_t *dh, int off, int len,
+                                       int w1, int w2, uint32_t e, Eval &r)
+{
+    const int32_t *L = d.lits + off;
+    int32_t l1 = L[w1], l2 = L[w2];
+    bool c1 = cons_of(asg[l1 >> 1], l1, e), c2 = cons_of(asg[l2 >> 1], l2, e);
+    r.acnt = 2;
+    r.act = A_NONE;
+    if (c1 && c2) return;
+    int pend = (!c1 && !c2) ? 2 : 1, f1 = -1, f2 = -1;
+    for (int i = 0; pend > 0 && i < len; i++) {
+        if (i == w1 || i == w2) continue;
+        int32_t l = L[i];
+        r.acnt++;
+        if (cons_of(asg[l >> 1], l, e)) {
+            if (f1 < 0) f1 = i;
+            else f2 = i;
+            pend--;
+        }
+    }
+    int32_t unit = -1;
+    if (c1 || c2) {
+        if (f1 < 0) {
+            unit = c1 ? l1 : l2;
+        } else {
+            r.act = A_SW1;
+            r.nw1 = c1 ? w1 : f1;
+            r.nw2 = c1 ? f1 : w2;
+            r.t1 = L[f1] >> 1;
+            r.dh1 = dh[r.t1];
+            return;
+        }
+    } else if (f1 >= 0 && f2 >= 0) {
+        r.act = A_SW2;
+        r.nw1 = f1;
+        r.nw2 = f2;
+        r.t1 = L[f1] >> 1;
+        r.t2 = L[f2] >> 1;
+        r.dh1 = dh[r.t1];
+        r.dh2 = dh[r.t2];
+        return;
+    } else if (f1 >= 0) {
+        unit = L[f1];
+    } else {
+        r.act = A_CONFLICT;
+        return;
+    }
+    r.unit = unit;
+    r.act = ((uint32_t)(asg[unit >> 1] >> 1) != e) ? A_IMPLY : A_BLOCK;
+}
+
+__device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int lane)
+{
+    uint8_t *asg = d.asg + (size_t)slot * d.n_pad;
+    uint32_t *cst = d.cst + (size_t)slot * d.m_pad;
+    uint32_t *dh = d.dh + (size_t)slot * d.n_pad;
+    int4 *arena = d.arena + (size_t)slot * d.arena_cap;
+    int2 *stk = d.stack + (size_t)slot * d.impl_cap;
+    int32_t *ilit = d.ilit + (size_t)t * d.impl_cap;
+    int32_t *ireason = d.ireason + (size_t)t * d.impl_cap;
+    const int32_t n = d.n_vars;
+
+    // ---- epoch of this slot
+    uint32_t e = 0;
+    if (lane == 0) e = d.epoch[slot] + 1;
+    e = __shfl_sync(FULL, e, 0);
+    if (e > EPMAX) {
+        uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *a4 = reinterpret_cast<uint4 *>(asg);
+        for (int64_t i = lane; i < d.n_pad / 16; i += 32) a4[i] = z;
+        uint4 *c4 = reinterpret_cast<uint4 *>(cst);
+        for (int64_t i = lane; i < d.m_pad / 4; i += 32) c4[i] = z;
+        uint4 *h4 = reinterpret_cast<uint4 *>(dh);
+        for (int64_t i = lane; i < d.n_pad / 4; i += 32) h4[i] = z;
+        e = 1;
+        __syncwarp();
+    }
+    if (lane == 0) d.epoch[slot] = e;
+
+    const int64_t tb = d.toff[t];
+    const int64_t tn = d.toff[t + 1] - tb;
+
+    // ---- assign every trail literal first
+    bool bad = tn < 0;
+    for (int64_t i = lane; i < tn; i += 32) {
+        int32_t x = d.trail[tb + i];
+        if (x == 0 || x > n || x < -n) bad = true;
+        else asg[(x > 0 ? x : -x) - 1] = (uint8_t)((e << 1) | (x > 0 ? 1u : 0u));
+    }
+    bad = __any_sync(FULL, bad);
+    __syncwarp();
+    if (!bad) {
+        // a variable given both signs leaves one of its literals unmatched
+        for (int64_t i = lane; i < tn; i += 32) {
+            int32_t x = d.trail[tb + i];
+            if (asg[(x > 0 ? x : -x) - 1] != (uint8_t)((e << 1) | (x > 0 ? 1u : 0u))) bad = true;
+        }
+        bad = __any_sync(FULL, bad);
+    }
+
+    int64_t n_impl = 0, props = 0, cW = 0, cL = 0, cA = 0, cI = 0;
+    int32_t status = bad ? GPSAT_BCP_BAD_TRAIL : GPSAT_BCP_NO_CONFLICT, confl = -1, stopi = -1;
+    int64_t arena_used = 0, ti = 0, top_j = 0, top_e = 0, cur_impl_start = 0, cur_trail = -1, dfs_trail = -1;
+    int depth = 0;
+    bool in_scan = false, cur_counted = false, cur_is_trail = false;
+    int32_t cur_var = 0, cur_dp = -1;
+    uint32_t cur_wk = 0, cur_wend = 0;
+    // every iteration finishes a scan, pops a frame or commits at least one
+    // entry; the budget only guarantees termination if that were ever broken
+    int64_t budget = MAX_ITERS;
+
+    while (status == GPSAT_BCP_NO_CONFLICT) {
+        if (--budget < 0) {
+            status = GPSAT_BCP_BUDGET;
+            stopi = (int32_t)cur_trail;
+            break;
+        }
+        if (!in_scan) {
+            int32_t v;
+            if (depth > 0) {
+                if (top_j < top_e) {
+                    int32_t x = ilit[top_j];
+                    top_j++;
+                    v = (x > 0 ? x : -x) - 1;
+                    cur_is_trail = false;
+                    cur_trail = dfs_trail;
+                } else {
+                    depth--;
+                    if (depth > 0) {
+                        int2 fr = stk[depth - 1];
+                        top_j = fr.x;
+                        top_e = fr.y;
+                    }
+                    continue;
+                }
+            } else {
+                if (ti >= tn) break;
+                int32_t x = d.trail[tb + ti];
+                v = (x > 0 ? x : -x) - 1;
+                cur_trail = ti;
+                dfs_trail = ti;
+                ti++;
+                cur_is_trail = true;
+            }
+            uint32_t h = dh[v];
+            cur_var = v;
+            cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+            cur_wk = d.w0off[v];
+            cur_wend = d.w0off[v + 1];
+            cur_counted = false;
+            cur_impl_start = n_impl;
+            in_scan = true;
+        }
+        if (!cur_counted) {
+            props++;
+            cur_counted = true;
+        }
+        if (cur_dp < 0 && cur_wk >= cur_wend) {
+            // scan finished: descend into the implications it found
+            in_scan = false;
+            if (n_impl > cur_impl_start) {
+                if (depth > 0 && lane == 0) stk[depth - 1] = make_int2((int)top_j, (int)top_e);
+                top_j = cur_impl_start;
+                top_e = n_impl;
+                depth++;
+            }
+            continue;
+        }
+
+        // ---- gather the window
+        int ndyn = 0;
+        bool dyn_done = true;
+        if (cur_dp >= 0) {
+            if (lane == 0) {
+                int32_t p = cur_dp;
+                while (p >= 0 && ndyn < 32) {
+                    int4 a = arena[p];
+                    sm.ent[ndyn] = a;
+                    p = a.w;
+                    sm.dp_after[ndyn] = p;
+                    ndyn++;
+                }
+                dyn_done = p < 0;
+            }
+            ndyn = __shfl_sync(FULL, ndyn, 0);
+            dyn_done = __shfl_sync(FULL, dyn_done, 0);
+        }
+        int nent = ndyn;
+        int take0 = 0;
+        if (dyn_done) {
+            take0 = min(32 - nent, (int)(cur_wend - cur_wk));
+            if (lane < take0) sm.ent[nent + lane] = d.w0ent[cur_wk + lane];
+            nent += take0;
+        }
+        if (lane == 0) {
+            sm.sc_var[0] = cur_var;
+            sm.sc_begin[0] = 0;
+            sm.sc_end[0] = nent;
+        }
+        int nsc = 1;
+        const bool scan0_full = dyn_done && (cur_wk + (uint32_t)take0 == cur_wend);
+        if (scan0_full && depth == 0 && cur_is_trail && n_impl == cur_impl_start && nent < 32 && ti < tn) {
+            const int room = 32 - nent;
+            const int nlook = (int)(tn - ti < 31 ? tn - ti : 31);
+            int32_t v = -1;
+            uint32_t a = 0, b = 0;
+            bool dynne = false;
+            if (lane < nlook) {
+                int32_t x = d.trail[tb + ti + lane];
+                v = (x > 0 ? x : -x) - 1;
+                uint32_t h = dh[v];
+                dynne = (h >> 24) == e;
+                a = d.w0off[v];
+                b = d.w0off[v + 1];
+            }
+            int cnt = (lane < nlook) ? (int)(b - a < 32u ? b - a : 32u) : 0;
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int excl = incl - cnt;
+            unsigned ok = __ballot_sync(FULL, lane < nlook && !dynne && excl < room);
+            int K = (~ok) ? __ffs(~ok) - 1 : 32;
+            if (lane < K) {
+                sm.sc_var[1 + lane] = v;
+                sm.sc_begin[1 + lane] = nent + excl;
+                sm.sc_end[1 + lane] = min(nent + excl + cnt, 32);
+                sm.sc_wk[1 + lane] = a;
+                sm.sc_wend[1 + lane] = b;
+            }
+            if (K > 0) {
+                int total = nent + __shfl_sync(FULL, incl, K - 1);
+                total = min(total, 32);
+                int q = lane - nent;
+                int s = 0;
+                for (int j = 1; j < K; j++) {
+                    int ej = __shfl_sync(FULL, excl, j);
+                    if (q >= ej) s = j;
+                }
+                int es = __shfl_sync(FULL, excl, s);
+                uint32_t as = __shfl_sync(FULL, a, s);
+                if (lane >= nent && lane < total) sm.ent[lane] = d.w0ent[as + (uint32_t)(q - es)];
+                nent = total;
+                nsc = 1 + K;
+            }
+        }
+        __syncwarp();
+
+        // ---- evaluate every entry of the window at once
+        const bool has = lane < nent;
+        int my_scan = 0;
+        for (int s = 1; s < nsc; s++)
+            if (lane >= sm.sc_begin[s]) my_scan = s;
+        const int4 en = has ? sm.ent[lane] : make_int4(0, 0, 0, 0);
+        const int32_t sv = sm.sc_var[my_scan];
+        Eval r;
+        r.act = A_NONE;
+        r.acnt = 0;
+        r.t1 = r.t2 = -1;
+        r.dh1 = r.dh2 = 0;
+        r.unit = -1;
+        r.nw1 = r.nw2 = 0;
+        bool valid = false;
+        int w1 = 0, w2 = 0;
+        if (has) {
+            const uint32_t st = cst[en.x];
+            const int len = en.z;
+            bool blk;
+            if ((st >> 24) == e) {
+                blk = (st >> 22) & 1u;
+                w1 = (st >> 11) & 0x7FFu;
+                w2 = st & 0x7FFu;
+            } else {
+                blk = false;
+                w1 = (uint32_t)en.w >> 16;
+                w2 = en.w & 0xFFFF;
+            }
+            if (len <= KREG) {
+                int32_t Lr[KREG];
+#pragma unroll
+                for (int i = 0; i < KREG; i++) Lr[i] = (i < len) ? d.lits[en.y + i] : 0;  // pad: a valid index
+                int32_t l1 = 0, l2 = 0;
+#pragma unroll
+                for (int i = 0; i < KREG; i++) {
+                    if (i == w1) l1 = Lr[i];
+                    if (i == w2) l2 = Lr[i];
+                }
+                valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
+                if (valid) {
+                    uint8_t Av[KREG];
+                    uint32_t Dh[KREG];
+#pragma unroll
+                    for (int i = 0; i < KREG; i++) {
+                        Av[i] = (i < len) ? asg[Lr[i] >> 1] : 0;
+                        Dh[i] = (i < len && i != w1 && i != w2) ? dh[Lr[i] >> 1] : 0;
+                    }
+                    bool c1 = false, c2 = false;
+#pragma unroll
+                    for (int i = 0; i < KREG; i++) {
+                        if (i == w1) c1 = cons_of(Av[i], Lr[i], e);
+                        if (i == w2) c2 = cons_of(Av[i], Lr[i], e);
+                    }
+                    r.acnt = 2;
+                    if (!(c1 && c2)) {
+                        int pend = (!c1 && !c2) ? 2 : 1, f1 = -1, f2 = -1;
+                        int32_t lf1 = 0, lf2 = 0;
+                        uint32_t df1 = 0, df2 = 0;
+                        uint8_t af1 = 0;
+#pragma unroll
+                        for (int i = 0; i < KREG; i++) {
+                            if (i < len && pend > 0 && i != w1 && i != w2) {
+                                r.acnt++;
+                                if (cons_of(Av[i], Lr[i], e)) {
+                                    if (f1 < 0) {
+                                        f1 = i;
+                                        lf1 = Lr[i];
+                                        df1 = Dh[i];
+                                        af1 = Av[i];
+                                    } else {
+                                        f2 = i;
+                                        lf2 = Lr[i];
+                                        df2 = Dh[i];
+                                    }
+                                    pend--;
+                                }
+                            }
+                        }
+                        int32_t unit = -1;
+                        uint8_t au = 0;
+                        if (c1 || c2) {
+                            if (f1 < 0) {
+                                unit = c1 ? l1 : l2;
+#pragma unroll
+                                for (int i = 0; i < KREG; i++)
+                                    if (i == (c1 ? w1 : w2)) au = Av[i];
+                            } else {
+                                r.act = A_SW1;
+                                r.nw1 = c1 ? w1 : f1;
+                                r.nw2 = c1 ? f1 : w2;
+                                r.t1 = lf1 >> 1;
+                                r.dh1 = df1;
+                            }
+                        } else if (f1 >= 0 && f2 >= 0) {
+                            r.act = A_SW2;
+                            r.nw1 = f1;
+                            r.nw2 = f2;
+                            r.t1 = lf1 >> 1;
+                            r.t2 = lf2 >> 1;
+                            r.dh1 = df1;
+                            r.dh2 = df2;
+                        } else if (f1 >= 0) {
+                            unit = lf1;
+                            au = af1;
+                        } else {
+                            r.act = A_CONFLICT;
+                        }
+                        if (unit >= 0) {
+                            r.unit = unit;
+                            r.act = ((uint32_t)(au >> 1) != e) ? A_IMPLY : A_BLOCK;
+                        }
+                    }
+                }
+            } else {
+                const int32_t l1 = d.lits[en.y + w1], l2 = d.lits[en.y + w2];
+                valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
+                if (valid) eval_long(d, asg, dh, en.y, len, w1, w2, e, r);
+            }
+        }
+
+        // ---- commit in reference order
+        const unsigned lt = lanemask_lt();
+        const int key = has ? en.x : -1 - lane;
+        const unsigned mm = __match_any_sync(FULL, key);
+        const unsigned dupmask = __ballot_sync(FULL, has && (mm & lt) != 0);
+        const unsigned sammask = __ballot_sync(FULL, valid && (r.act == A_IMPLY || r.act == A_CONFLICT));
+        const bool isw = valid && (r.act == A_SW1 || r.act == A_SW2);
+        int k_end = nent, new_cur = 0;
+        bool new_started = true;
+        for (int s = 0; s < nsc; s++) {
+            const int b = sm.sc_begin[s], eo = sm.sc_end[s];
+            if (s >= 1) {
+                const int32_t vs = sm.sc_var[s];
+                unsigned hit = __ballot_sync(FULL, isw && lane < b && (r.t1 == vs || r.t2 == vs));
+                if (hit) {
+                    k_end = b;
+                    new_cur = s;
+                    new_started = false;
+                    break;
+                }
+            }
+            const unsigned rg = range_mask(b, eo);
+            const unsigned dm = dupmask & rg, smk = sammask & rg;
+            const int fd = dm ? __ffs(dm) - 1 : 32;
+            const int fs = smk ? __ffs(smk) - 1 : 32;
+            if (fd < 32 || fs < 32) {
+                new_cur = s;
+                if (fd <= fs) {
+                    k_end = fd;
+                    new_started = (s == 0) || (fd > b);
+                } else {
+                    k_end = fs + 1;
+                    new_started = true;
+                }
+                break;
+            }
+            if (s == nsc - 1) {
+                k_end = eo;
+                new_cur = s;
+                new_started = (s == 0) || (eo > b);
+            }
+        }
+
+        const bool com = valid && lane < k_end;
+        // watch moves: add_first into the target var's list, in commit order
+        const bool ins1 = com && (r.act == A_SW1 || r.act == A_SW2);
+        const bool ins2 = com && r.act == A_SW2;
+        const unsigned m1 = __ballot_sync(FULL, ins1), m2 = __ballot_sync(FULL, ins2);
+        const int total_ins = __popc(m1) + __popc(m2);
+        if (arena_used + total_ins > d.arena_cap) {
+            status = GPSAT_BCP_OVERFLOW;
+            stopi = (int32_t)cur_trail;
+            break;
+        }
+        const unsigned imask = __ballot_sync(FULL, com && r.act == A_IMPLY);
+        if (imask && n_impl >= d.impl_cap) {
+            status = GPSAT_BCP_OVERFLOW;
+            stopi = (int32_t)cur_trail;
+            break;
+        }
+        if (m2 == 0) {
+            const int myidx = (int)arena_used + __popc(m1 & lt);
+            const unsigned g = __match_any_sync(FULL, ins1 ? r.t1 : -1 - lane);
+            if (ins1) {
+                const unsigned before = g & lt;
+                int32_t next;
+                if (before) {
+                    const int pl = 31 - __clz(before);
+                    next = (int)arena_used + __popc(m1 & ((1u << pl) - 1u));
+                } else {
+                    next = ((r.dh1 >> 24) == e) ? (int32_t)(r.dh1 & 0xFFFFFFu) : -1;
+                }
+                arena[myidx] = make_int4(en.x, en.y, en.z, next);
+                if ((g & lanemask_gt()) == 0) dh[r.t1] = (e << 24) | (uint32_t)myidx;
+            }
+        } else {
+            // rare (a clause moving both watches needs 4+ literals): lane 0
+            // inserts every move serially, in commit order
+            int idx = (int)arena_used;
+            unsigned rem = m1;
+            while (rem) {
+                const int k = __ffs(rem) - 1;
+                rem &= rem - 1;
+                const int32_t c = __shfl_sync(FULL, en.x, k), off = __shfl_sync(FULL, en.y, k),
+                              len = __shfl_sync(FULL, en.z, k);
+                const int32_t tt1 = __shfl_sync(FULL, r.t1, k), tt2 = __shfl_sync(FULL, r.t2, k);
+                const bool two = (m2 >> k) & 1u;
+                if (lane == 0) {
+                    uint32_t h = dh[tt1];
+                    int32_t next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+                    arena[idx] = make_int4(c, off, len, next);
+                    dh[tt1] = (e << 24) | (uint32_t)idx;
+                    if (two) {
+                        h = dh[tt2];
+                        next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+                        arena[idx + 1] = make_int4(c, off, len, next);
+                        dh[tt2] = (e << 24) | (uint32_t)(idx + 1);
+                    }
+                }
+                idx += two ? 2 : 1;
+            }
+        }
+        arena_used += total_ins;
+
+        // clause states
+        if (com && r.act != A_NONE) {
+            uint32_t ns;
+            if (r.act == A_SW1 || r.act == A_SW2) ns = (e << 24) | ((uint32_t)r.nw1 << 11) | (uint32_t)r.nw2;
+            else ns = (e << 24) | (1u << 22) | ((uint32_t)w1 << 11) | (uint32_t)w2;
+            cst[en.x] = ns;
+        }
+        // implication (at most one per round: it ends the commit)
+        if (imask) {
+            const int k = __ffs(imask) - 1;
+            if (lane == k) {
+                ilit[n_impl] = dimacs_of(r.unit);
+                ireason[n_impl] = en.x;
+                asg[r.unit >> 1] = (uint8_t)((e << 1) | (uint32_t)(r.unit & 1));
+            }
+            n_impl++;
+            cI++;
+        }
+        const unsigned cmask = __ballot_sync(FULL, com && r.act == A_CONFLICT);
+        cW += __popc(__ballot_sync(FULL, com));
+        cL += warp_sum(com ? en.z : 0);
+        cA += warp_sum(com ? r.acnt : 0);
+        const int64_t ti_round = ti;
+        __syncwarp();
+
+        // ---- advance the scan cursors
+        if (new_cur == 0) {
+            if (k_end > 0) {
+                if (k_end <= ndyn) {
+                    cur_dp = sm.dp_after[k_end - 1];
+                } else {
+                    cur_dp = -1;
+                    cur_wk += (uint32_t)(k_end - ndyn);
+                }
+            }
+        } else {
+            props += new_cur - 1;
+            cur_var = sm.sc_var[new_cur];
+            cur_dp = -1;
+            cur_wk = sm.sc_wk[new_cur] + (uint32_t)(k_end - sm.sc_begin[new_cur]);
+            cur_wend = sm.sc_wend[new_cur];
+            cur_counted = new_started;
+            if (new_started) props++;
+            cur_trail = ti + new_cur - 1;
+            dfs_trail = cur_trail;
+            ti += new_cur;
+            cur_is_trail = true;
+            cur_impl_start = n_impl - (imask ? 1 : 0);
+        }
+        if (cmask) {
+            const int k = __ffs(cmask) - 1;
+            confl = __shfl_sync(FULL, en.x, k);
+            const int ks = __shfl_sync(FULL, my_scan, k);
+            stopi = (int32_t)(ks == 0 ? (new_cur == 0 ? cur_trail : dfs_trail) : ti_round + ks - 1);
+            status = GPSAT_BCP_CONFLICT;
+        }
+        __syncwarp();
+    }
+
+    if (lane == 0) {
+        d.status[t] = status;
+        d.conflict[t] = confl;
+        d.stop[t] = stopi;
+        d.nimpl[t] = n_impl;
+        if (d.counters) {
+            int64_t *cn = d.counters + (size_t)t * GPSAT_BCP_NCOUNTERS;
+            cn[0] = props;
+            cn[1] = cW;
+            cn[2] = cL;
+            cn[3] = cA;
+            cn[4] = cI;
+            cn[5] = bad ? 0 : tn;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(WARPS * 32, 8) bcp_kernel(Dev d)
+{
+    __shared__ WarpSmem smem[WARPS];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int slot = blockIdx.x * WARPS + wib;
+    if (slot >= d.n_slots) return;
+    while (true) {
+        int t = 0;
+        if (lane == 0) t = (int)atomicAdd(d.next_trail, 1u);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= d.n_trails) break;
+        process_trail(d, smem[wib], t, slot, lane);
+    }
+}
+
+}  // namespace bcp
+}  // namespace gpsat
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace gpsat;
+
+struct gpsat_bcp {
+    const gpsat_formula *f = nullptr;
+    int device = 0;
+    int32_t slots = 0;
+    int64_t n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
+    uint8_t *asg = nullptr;
+    uint32_t *cst = nullptr, *dh = nullptr, *epoch = nullptr;
+    int4 *arena = nullptr;
+    int2 *stack = nullptr;
+    unsigned int *counter = nullptr;
+    int64_t bytes = 0;
+    // host-path staging
+    int32_t *d_trail = nullptr;
+    int64_t *d_toff = nullptr;
+    int64_t trail_cap = 0, toff_cap = 0;
+    void *d_out = nullptr;
+    int64_t out_cap = 0;
+};
+
+namespace {
+
+void bcp_free(gpsat_bcp *b)
+{
+    cudaFree(b->asg);
+    cudaFree(b->cst);
+    cudaFree(b->dh);
+    cudaFree(b->epoch);
+    cudaFree(b->arena);
+    cudaFree(b->stack);
+    cudaFree(b->counter);
+    cudaFree(b->d_trail);
+    cudaFree(b->d_toff);
+    cudaFree(b->d_out);
+}
+
+int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, int32_t *status,
+           int32_t *conflict, int32_t *stop, int64_t *nimpl, int32_t *ilit, int32_t *ireason, int64_t *counters,
+           cudaStream_t st)
+{
+    const gpsat_formula *f = b->f;
+    bcp::Dev d;
+    d.n_vars = f->h.n_vars;
+    d.n_clauses = (int32_t)f->h.n_clauses();
+    d.lits = f->d_lits;
+    d.w0off = f->d_w0off;
+    d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
+    d.asg = b->asg;
+    d.cst = b->cst;
+    d.dh = b->dh;
+    d.arena = b->arena;
+    d.stack = b->stack;
+    d.epoch = b->epoch;
+    d.next_trail = b->counter;
+    d.n_pad = b->n_pad;
+    d.m_pad = b->m_pad;
+    d.arena_cap = b->arena_cap;
+    d.impl_cap = b->impl_cap;
+    d.n_slots = std::min<int32_t>(b->slots, std::max<int32_t>(n_trails, 1));
+    d.trail = trail;
+    d.toff = toff;
+    d.n_trails = n_trails;
+    d.status = status;
+    d.conflict = conflict;
+    d.stop = stop;
+    d.nimpl = nimpl;
+    d.ilit = ilit;
+    d.ireason = ireason;
+    d.counters = counters;
+    cudaError_t err = cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), st);
+    if (err != cudaSuccess) return cuda_error(err, "bcp counter reset");
+    if (n_trails == 0) return GPSAT_OK;
+    const int blocks = (d.n_slots + bcp::WARPS - 1) / bcp::WARPS;
+    bcp::bcp_kernel<<<blocks, bcp::WARPS * 32, 0, st>>>(d);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch");
+    return GPSAT_OK;
+}
+
+}  // namespace
+
+extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64_t impl_cap, int64_t arena_cap,
+                                gpsat_bcp **out)
+{
+    if (!f || !out || impl_cap <= 0 || impl_cap > INT32_MAX || max_slots < 0 || arena_cap < 0 ||
+        arena_cap > (1 << 24))
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_create: bad argument");
+    *out = nullptr;
+    if (f->h.verdict != GPSAT_UNKNOWN)
+        return set_error(GPSAT_ERR_STATE, "formula was decided by preprocessing; nothing to propagate");
+    if (f->h.max_len > bcp::MAXLEN)
+        return set_error(GPSAT_ERR_CAPACITY, "clause longer than 2048 literals");
+    int urc = formula_upload(const_cast<gpsat_formula *>(f));
+    if (urc != GPSAT_OK) return urc;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::WARPS * 32, 0);
+    int32_t resident = std::max(1, sms * std::max(per_sm, 1) * bcp::WARPS);
+    gpsat_bcp *b = new gpsat_bcp();
+    b->f = f;
+    b->device = f->device;
+    b->n_pad = ((int64_t)f->h.n_vars + 15) / 16 * 16;
+    b->m_pad = (f->h.n_clauses() + 3) / 4 * 4;
+    b->impl_cap = impl_cap;
+    b->arena_cap = arena_cap ? arena_cap : (1 << 17);
+    const int64_t per_slot = b->n_pad * 5 + b->m_pad * 4 + b->arena_cap * 16 + b->impl_cap * 8;
+    int32_t slots = max_slots ? max_slots : resident;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const int64_t budget = (int64_t)(free_b * 0.6);
+    if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
+    b->slots = slots;
+    const size_t S = (size_t)slots;
+    bool ok = cudaMalloc(&b->asg, S * b->n_pad) == cudaSuccess &&
+              cudaMalloc(&b->cst, S * b->m_pad * 4) == cudaSuccess &&
+              cudaMalloc(&b->dh, S * b->n_pad * 4) == cudaSuccess &&
+              cudaMalloc(&b->epoch, S * 4) == cudaSuccess &&
+              cudaMalloc(&b->arena, S * b->arena_cap * 16) == cudaSuccess &&
+              cudaMalloc(&b->stack, S * b->impl_cap * 8) == cudaSuccess &&
+              cudaMalloc(&b->counter, 16) == cudaSuccess;
+    if (ok)
+        ok = cudaMemset(b->asg, 0, S * b->n_pad) == cudaSuccess &&
+             cudaMemset(b->cst, 0, S * b->m_pad * 4) == cudaSuccess &&
+             cudaMemset(b->dh, 0, S * b->n_pad * 4) == cudaSuccess && cudaMemset(b->epoch, 0, S * 4) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        bcp_free(b);
+        delete b;
+        return set_error(GPSAT_ERR_NOMEM, "gpsat_bcp_create: device allocation failed");
+    }
+    b->bytes = (int64_t)S * per_slot;
+    *out = b;
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_bcp_destroy(gpsat_bcp *b)
+{
+    if (!b) return GPSAT_OK;
+    cudaSetDevice(b->device);
+    bcp_free(b);
+    delete b;
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes)
+{
+    if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
+    if (slots) *slots = b->slots;
+    if (device_bytes) *device_bytes = b->bytes;
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
+                                    int32_t n_trails, int32_t *status, int32_t *conflict_clause,
+                                    int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,
+                                    int32_t *impl_reason, int64_t *counters, void *stream)
+{
+    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index ||
+                                                !n_impl || !impl_lit || !impl_reason)))
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_device: bad argument");
+    cudaError_t err = cudaSetDevice(b->device);
+    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    return launch(b, trail_lits, trail_offsets, n_trails, status, conflict_clause, stop_index, n_impl, impl_lit,
+                  impl_reason, counters, (cudaStream_t)stream);
+}
+
+extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
+                                  int32_t n_trails, int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                                  int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
+{
+    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index ||
+                                                !n_impl || !impl_lit || !impl_reason)))
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_host: bad argument");
+    if (n_trails == 0) return GPSAT_OK;
+    cudaError_t err = cudaSetDevice(b->device);
+    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    const int64_t nl = trail_offsets[n_trails];
+    if (nl < 0 || (nl > 0 && !trail_lits)) return set_error(GPSAT_ERR_ARG, "bad trail offsets");
+    if (nl > b->trail_cap) {
+        cudaFree(b->d_trail);
+        b->d_trail = nullptr;
+        if (cudaMalloc(&b->d_trail, std::max<int64_t>(nl, 1) * 4) != cudaSuccess) {
+            b->trail_cap = 0;
+            return set_error(GPSAT_ERR_NOMEM, "trail staging");
+        }
+        b->trail_cap = nl;
+    }
+    if (n_trails + 1 > b->toff_cap) {
+        cudaFree(b->d_toff);
+        b->d_toff = nullptr;
+        if (cudaMalloc(&b->d_toff, (int64_t)(n_trails + 1) * 8) != cudaSuccess) {
+            b->toff_cap = 0;
+            return set_error(GPSAT_ERR_NOMEM, "offset staging");
+        }
+        b->toff_cap = n_trails + 1;
+    }
+    const int64_t T = n_trails;
+    const int64_t need = T * (4 + 4 + 4 + 8 + 8 * GPSAT_BCP_NCOUNTERS) + 2 * T * b->impl_cap * 4 + 64;
+    if (need > b->out_cap) {
+        cudaFree(b->d_out);
+        b->d_out = nullptr;
+        if (cudaMalloc(&b->d_out, need) != cudaSuccess) {
+            b->out_cap = 0;
+            return set_error(GPSAT_ERR_NOMEM, "output staging");
+        }
+        b->out_cap = need;
+    }
+    char *p = (char *)b->d_out;
+    int64_t *d_nimpl = (int64_t *)p;
+    p += T * 8;
+    int64_t *d_cnt = (int64_t *)p;
+    p += T * 8 * GPSAT_BCP_NCOUNTERS;
+    int32_t *d_status = (int32_t *)p;
+    p += T * 4;
+    int32_t *d_confl = (int32_t *)p;
+    p += T * 4;
+    int32_t *d_stop = (int32_t *)p;
+    p += T * 4;
+    int32_t *d_ilit = (int32_t *)p;
+    p += T * b->impl_cap * 4;
+    int32_t *d_ireason = (int32_t *)p;
+    cudaStream_t st = 0;
+    if (nl > 0 && cudaMemcpyAsync(b->d_trail, trail_lits, nl * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return cuda_error(cudaGetLastError(), "trail copy");
+    if (cudaMemcpyAsync(b->d_toff, trail_offsets, (T + 1) * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return cuda_error(cudaGetLastError(), "offset copy");
+    int rc = launch(b, b->d_trail, b->d_toff, n_trails, d_status, d_confl, d_stop, d_nimpl, d_ilit, d_ireason,
+                    counters ? d_cnt : nullptr, st);
+    if (rc != GPSAT_OK) return rc;
+    bool ok = cudaMemcpyAsync(status, d_status, T * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+              cudaMemcpyAsync(conflict_clause, d_confl, T * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+              cudaMemcpyAsync(stop_index, d_stop, T * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+              cudaMemcpyAsync(n_impl, d_nimpl, T * 8, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    if (ok && counters)
+        ok = cudaMemcpyAsync(counters, d_cnt, T * 8 * GPSAT_BCP_NCOUNTERS, cudaMemcpyDeviceToHost, st) ==
+             cudaSuccess;
+    if (!ok) return cuda_error(cudaGetLastError(), "result copy");
+    err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) return cuda_error(err, "bcp run");
+    // implication lists: copy only the used prefix of each trail's region
+    int64_t maxn = 0;
+    for (int64_t t = 0; t < T; t++) maxn = std::max(maxn, n_impl[t]);
+    if (maxn * 4 >= b->impl_cap * 2) {
+        ok = cudaMemcpy(impl_lit, d_ilit, T * b->impl_cap * 4, cudaMemcpyDeviceToHost) == cudaSuccess &&
+             cudaMemcpy(impl_reason, d_ireason, T * b->impl_cap * 4, cudaMemcpyDeviceToHost) == cudaSuccess;
+    } else if (maxn > 0) {
+        ok = cudaMemcpy2D(impl_lit, b->impl_cap * 4, d_ilit, b->impl_cap * 4, maxn * 4, T,
+                          cudaMemcpyDeviceToHost) == cudaSuccess &&
+             cudaMemcpy2D(impl_reason, b->impl_cap * 4, d_ireason, b->impl_cap * 4, maxn * 4, T,
+                          cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    if (!ok) return cuda_error(cudaGetLastError(), "implication copy");
+    return GPSAT_OK;
+}

@@ -1,0 +1,96 @@
+"""ORACLE -- test infrastructure only.
+
+CPU checkers for the gpsat GPU path.  Only tests/, __graft_entry__.smoke()
+and the CPU-baseline leg of bench.py import this package; the shipped
+library never does.
+
+  bcp_ref.c   C restatement of the reference's two-watched-literal BCP in its
+              own processing order (see the file header for the cited lines)
+  ref/        recipe that compiles the reference's own solver sources for the
+              host (output: oracle/_ref/), used to pin the restatement
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+SOURCES = [HERE / "bcp_ref.c"]
+
+_lib = None
+_vp = ctypes.c_void_p
+
+
+def build() -> Path:
+    """Compiles the C restatement (gcc, portable flags, no arch tuning)."""
+    if not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in SOURCES):
+        cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", *map(str, SOURCES), "-o", str(LIB)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        L.orc_bcp_create.restype = _vp
+        L.orc_bcp_create.argtypes = [_vp, _vp, ctypes.c_int32, ctypes.c_int64]
+        L.orc_bcp_destroy.argtypes = [_vp]
+        L.orc_bcp_initial_watches.argtypes = [_vp, _vp, _vp]
+        L.orc_bcp_run.argtypes = [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64] + [_vp] * 7
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class BCPOracle:
+    """Reference-order BCP on the CPU. Clauses must be clean (length >= 2, distinct variables)."""
+
+    def __init__(self, lits: np.ndarray, offsets: np.ndarray, n_vars: int):
+        self._lits = np.ascontiguousarray(lits, dtype=np.int32)
+        self._off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.n_clauses = len(self._off) - 1
+        self._h = lib().orc_bcp_create(_p(self._lits), _p(self._off), n_vars, self.n_clauses)
+        if not self._h:
+            raise ValueError("oracle rejected the formula (needs clean clauses of length >= 2)")
+
+    def initial_watches(self):
+        w1 = np.empty(self.n_clauses, np.int32)
+        w2 = np.empty(self.n_clauses, np.int32)
+        lib().orc_bcp_initial_watches(self._h, _p(w1), _p(w2))
+        return w1, w2
+
+    def run(self, trail_lits: np.ndarray, trail_offsets: np.ndarray, impl_cap: int = 4096, threads: int = 1) -> dict:
+        trail_lits = np.ascontiguousarray(trail_lits, dtype=np.int32)
+        trail_offsets = np.ascontiguousarray(trail_offsets, dtype=np.int64)
+        T = len(trail_offsets) - 1
+        out = dict(status=np.empty(T, np.int32), conflict=np.empty(T, np.int32), stop=np.empty(T, np.int32),
+                   n_impl=np.empty(T, np.int64), impl_lit=np.zeros((T, impl_cap), np.int32),
+                   impl_reason=np.zeros((T, impl_cap), np.int32), counters=np.zeros((T, 6), np.int64))
+        rc = lib().orc_bcp_run(self._h, _p(trail_lits), _p(trail_offsets), T, threads, impl_cap,
+                               _p(out["status"]), _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
+                               _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out["counters"]))
+        if rc != 0:
+            raise RuntimeError(f"oracle run failed: {rc}")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().orc_bcp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

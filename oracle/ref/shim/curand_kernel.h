@@ -1,0 +1,2 @@
+#pragma once
+#include "cuda_shim_pre.h"

@@ -1,0 +1,82 @@
+"""CPU: the C-ABI library loads, exports every symbol include/gpsat.h declares,
+and its host-side parts (validation, preprocessing, generators, errors)
+behave; no kernel is launched here."""
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions(header):
+    text = (ROOT / "include" / header).read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gpsat_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(gpsat):
+    lib = ctypes.CDLL(str(gpsat.LIB_PATH))
+    names = declared_functions("gpsat.h")
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_version_and_errors(gpsat):
+    assert "sm_103a" in gpsat.version()
+    L = gpsat.lib()
+    assert L.gpsat_error_string(-6).decode() == "size exceeds a limit"
+    h = ctypes.c_void_p()
+    rc = L.gpsat_formula_create(None, None, 0, 0, ctypes.byref(h))
+    assert rc == -1 and not h
+    assert "n_vars" in L.gpsat_last_error().decode()
+
+
+def test_formula_validation(gpsat):
+    with pytest.raises(gpsat.GpsatError) as e:
+        gpsat.Formula(np.array([1, 5], np.int32), np.array([0, 2], np.int64), 3)
+    assert e.value.code == -4
+    with pytest.raises(gpsat.GpsatError) as e:
+        gpsat.Formula(np.array([1, 2], np.int32), np.array([0, 0, 2], np.int64), 3)  # empty clause
+    assert e.value.code == -4
+
+
+def test_preprocessing_decides_trivial_formulas(gpsat):
+    assert gpsat.Formula.from_clauses([[1, -1], [2, -2, 3]]).info()["verdict"] == gpsat.SAT
+    assert gpsat.Formula.from_clauses([[1], [-1], [1, 2]]).info()["verdict"] == gpsat.UNSAT
+    f = gpsat.Formula.from_clauses([[1], [-1, 2, 3], [-2, 3, 4], [2, 2, -4]])
+    ex = f.export()
+    assert ex["verdict"] == 0
+    assert list(ex["solved"]) == [1]
+    assert list(ex["lits"]) == [2, 3, -2, 3, 4, 2, -4]
+
+
+def test_generators_are_seeded_and_valid(gpsat):
+    a, off = gpsat.gen_random_ksat(5, 100, 400, 3)
+    b, _ = gpsat.gen_random_ksat(5, 100, 400, 3)
+    c, _ = gpsat.gen_random_ksat(6, 100, 400, 3)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    cl = np.abs(a.reshape(-1, 3))
+    assert (cl >= 1).all() and (cl <= 100).all()
+    assert all(len(set(r)) == 3 for r in cl.tolist())
+    assert 0.4 < (a > 0).mean() < 0.6
+    tl, to = gpsat.gen_trails(9, 1000, 50, 0.01, 0.05)
+    tl2, to2 = gpsat.gen_trails(9, 1000, 50, 0.01, 0.05)
+    assert np.array_equal(tl, tl2) and np.array_equal(to, to2)
+    lens = np.diff(to)
+    assert lens.min() >= 10 and lens.max() <= 50
+    for t in range(50):
+        v = np.abs(tl[to[t]:to[t + 1]])
+        assert len(np.unique(v)) == len(v) and v.min() >= 1 and v.max() <= 1000
+
+
+def test_bcp_without_device_fails_loudly(gpsat):
+    if gpsat.device_count() > 0:
+        pytest.skip("a GPU is visible; covered by the GPU tests")
+    lits, off = gpsat.gen_random_ksat(1, 50, 200, 3)
+    f = gpsat.Formula(lits, off, 50)
+    with pytest.raises(gpsat.GpsatError) as e:
+        gpsat.BCPBatch(f, impl_cap=64)
+    assert e.value.code == -7
