@@ -29,6 +29,21 @@ _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
 
 
+DECIDE_VSIDS, DECIDE_LAST_FREE = 0, 1
+RESTART_NONE, RESTART_LUBY, RESTART_GEOMETRIC = 0, 1, 2
+SOLVE_STAT_NAMES = ("conflicts", "decisions", "propagations", "restarts", "learnts", "reductions", "rebuilds",
+                    "flags", "jobs")
+
+
+class SolveOptions(ctypes.Structure):
+    _fields_ = [("decide", ctypes.c_int32), ("restart", ctypes.c_int32), ("restart_base", ctypes.c_int32),
+                ("restart_factor", ctypes.c_float), ("var_decay", ctypes.c_float),
+                ("learnt_first", ctypes.c_int32), ("learnt_inc", ctypes.c_int32), ("minimize", ctypes.c_int32),
+                ("conflict_budget", ctypes.c_int64), ("phase_init", ctypes.c_int32),
+                ("max_slots", ctypes.c_int32), ("log_participation", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
+
+
 class GpsatError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"gpsat error {code}: {msg}")
@@ -62,6 +77,14 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_bcp_info": (ctypes.c_int, [_vp, _c_i32p, _c_i64p]),
         "gpsat_bcp_run_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 8),
         "gpsat_bcp_run_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 7),
+        "gpsat_solve_options_default": (ctypes.c_int, [ctypes.POINTER(SolveOptions)]),
+        "gpsat_batch_create": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
+        "gpsat_batch_destroy": (ctypes.c_int, [_vp]),
+        "gpsat_batch_info": (ctypes.c_int, [_vp, _c_i32p, _c_i64p, _c_i32p, _c_i64p]),
+        "gpsat_batch_set_seeds": (ctypes.c_int, [_vp, _vp, _vp]),
+        "gpsat_batch_solve": (ctypes.c_int, [_vp, ctypes.POINTER(SolveOptions), _vp, _vp, _vp, ctypes.c_int32]
+                              + [_vp] * 5),
+        "gpsat_check_model": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int32, _c_i64p]),
         "gpsat_gen_random_ksat": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]),
         "gpsat_gen_trails": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                             ctypes.c_double, _vp, _vp]),
@@ -211,6 +234,107 @@ class BCPBatch:
     def close(self) -> None:
         if self._h:
             lib().gpsat_bcp_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- CDCL solving
+def solve_options(**kw) -> SolveOptions:
+    o = SolveOptions()
+    check(lib().gpsat_solve_options_default(ctypes.byref(o)))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def check_model(lits: np.ndarray, offsets: np.ndarray, model: np.ndarray, n_vars: int) -> bool:
+    """Host model check (independent of the device checker)."""
+    lits = np.ascontiguousarray(lits, np.int32)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    model = np.ascontiguousarray(model, np.int8)
+    bad = ctypes.c_int64(-1)
+    rc = lib().gpsat_check_model(_p(lits), _p(offsets), len(offsets) - 1, _p(model), n_vars, ctypes.byref(bad))
+    if rc < 0:
+        check(rc)
+    return rc == 1
+
+
+class Batch:
+    """Many formulas solved on the GPU by the device CDCL solver (one warp per job)."""
+
+    def __init__(self, formulas, n_vars):
+        """formulas: list of (lits, offsets) CSR pairs (DIMACS literals); n_vars: list of ints."""
+        self.n_vars = np.asarray(n_vars, np.int32)
+        offs = [np.asarray(o, np.int64) for _, o in formulas]
+        lits = np.concatenate([np.asarray(l, np.int32) for l, _ in formulas]) if formulas else np.zeros(0, np.int32)
+        coff = np.zeros(sum(len(o) - 1 for o in offs) + 1, np.int64)
+        foff = np.zeros(len(formulas) + 1, np.int64)
+        c = 0
+        base = 0
+        for i, o in enumerate(offs):
+            k = len(o) - 1
+            coff[c + 1:c + k + 1] = o[1:] + base
+            base += int(o[-1])
+            c += k
+            foff[i + 1] = c
+        self.clause_lits, self.clause_offsets, self.formula_offsets = lits, coff, foff
+        self.var_off = np.zeros(len(formulas) + 1, np.int64)
+        self.var_off[1:] = np.cumsum(self.n_vars)
+        self._h = _vp()
+        check(lib().gpsat_batch_create(_p(lits), _p(coff), _p(foff), _p(self.n_vars), len(formulas),
+                                       ctypes.byref(self._h)))
+
+    @property
+    def n_formulas(self) -> int:
+        return len(self.n_vars)
+
+    def formula(self, f: int):
+        c0, c1 = self.formula_offsets[f], self.formula_offsets[f + 1]
+        o = self.clause_offsets[c0:c1 + 1]
+        return self.clause_lits[o[0]:o[-1]], o - o[0]
+
+    def info(self) -> dict:
+        nf, tv, s, wb = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int64()
+        check(lib().gpsat_batch_info(self._h, ctypes.byref(nf), ctypes.byref(tv), ctypes.byref(s), ctypes.byref(wb)))
+        return dict(n_formulas=nf.value, total_vars=tv.value, slots=s.value, workspace_bytes=wb.value)
+
+    def set_seeds(self, activity=None, phase=None) -> None:
+        a = None if activity is None else np.ascontiguousarray(activity, np.float32)
+        p = None if phase is None else np.ascontiguousarray(phase, np.int8)
+        check(lib().gpsat_batch_set_seeds(self._h, _p(a), _p(p)))
+
+    def solve(self, options: SolveOptions | None = None, jobs=None, participation: bool = False) -> dict:
+        """jobs: None, or (job_formula int32[J], cube_offsets int64[J+1], cube_lits int32[...])."""
+        F = self.n_formulas
+        o = options or solve_options()
+        if participation:
+            o.log_participation = 1
+        out = dict(verdict=np.zeros(F, np.int32), model=np.zeros(int(self.var_off[-1]), np.int8),
+                   stats=np.zeros((F, 9), np.int64), model_ok=np.zeros(F, np.int32),
+                   participation=np.zeros(int(self.var_off[-1]), np.int32) if participation else None)
+        jf = co = cl = None
+        nj = 0
+        if jobs is not None:
+            jf = np.ascontiguousarray(jobs[0], np.int32)
+            co = np.ascontiguousarray(jobs[1], np.int64)
+            cl = np.ascontiguousarray(jobs[2], np.int32)
+            nj = len(jf)
+        check(lib().gpsat_batch_solve(self._h, ctypes.byref(o), _p(jf), _p(co), _p(cl), nj, _p(out["verdict"]),
+                                      _p(out["model"]), _p(out["stats"]), _p(out["model_ok"]),
+                                      _p(out["participation"])))
+        return out
+
+    def model_of(self, out: dict, f: int) -> np.ndarray:
+        return out["model"][self.var_off[f]:self.var_off[f + 1]]
+
+    def close(self) -> None:
+        if self._h:
+            lib().gpsat_batch_destroy(self._h)
             self._h = _vp()
 
     def __del__(self):

@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -17,7 +18,7 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
-BUILD = PKG / "_build"
+BUILD = PKG / "_build" / platform.machine()  # objects never cross architectures
 LIB = PKG / "libgpsat.so"
 CLI = PKG / "gpsat"
 
@@ -54,7 +55,7 @@ def _run(cmd: list[str]) -> None:
 def build(verbose: bool = False, jobs: int | None = None) -> Path:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
-    BUILD.mkdir(exist_ok=True)
+    BUILD.mkdir(parents=True, exist_ok=True)
     hdrs = _headers()
     inc = ["-I", str(CSRC), "-I", str(ROOT / "include")]
     cmds = []
@@ -76,9 +77,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     if cmds:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(cmds), os.cpu_count() or 4)) as ex:
             list(ex.map(_run, cmds))
-    if cmds or not LIB.exists():
+    stamp = BUILD / "libgpsat.stamp"
+    if cmds or not LIB.exists() or not stamp.exists() or stamp.stat().st_mtime < LIB.stat().st_mtime - 1:
         _run(["g++", "-shared", "-o", str(LIB), *map(str, objs), "-L", str(cuda / "lib64"),
               "-Wl,-rpath," + str(cuda / "lib64"), "-lcudart", "-pthread"])
+        stamp.write_text(platform.machine() + "\n")
     cli_src = CSRC / "cli_main.cpp"
     if cli_src.exists() and (_stale(cli_src, CLI, hdrs + [LIB]) or cmds):
         _run(["g++", "-O2", "-std=c++17", "-pthread", *inc, str(cli_src), "-o", str(CLI), "-L", str(PKG),

@@ -110,14 +110,19 @@ int formula_upload(gpsat_formula *f)
     const int64_t m = h.n_clauses();
     std::vector<uint32_t> coff(m + 1);
     for (int64_t c = 0; c <= m; c++) coff[c] = (uint32_t)h.off[c];
-    std::vector<int32_t> ent((size_t)h.w0off[h.n_vars] * 4);
+    // one 32-byte entry per initial watch: {clause, literal offset, length,
+    // (w1 << 16) | w2} then the clause's first four literals (0-padded)
+    std::vector<int32_t> ent((size_t)h.w0off[h.n_vars] * 8);
     for (int32_t v = 0; v < h.n_vars; v++) {
         for (uint32_t k = h.w0off[v]; k < h.w0off[v + 1]; k++) {
             int32_t c = h.w0cl[k];
-            ent[4 * (size_t)k + 0] = c;
-            ent[4 * (size_t)k + 1] = (int32_t)h.off[c];
-            ent[4 * (size_t)k + 2] = (int32_t)(h.off[c + 1] - h.off[c]);
-            ent[4 * (size_t)k + 3] = (int32_t)(((uint32_t)h.w1[c] << 16) | (uint32_t)h.w2[c]);
+            int32_t *e = &ent[8 * (size_t)k];
+            const int64_t b = h.off[c], len = h.off[c + 1] - b;
+            e[0] = c;
+            e[1] = (int32_t)b;
+            e[2] = (int32_t)len;
+            e[3] = (int32_t)(((uint32_t)h.w1[c] << 16) | (uint32_t)h.w2[c]);
+            for (int i = 0; i < 4; i++) e[4 + i] = i < len ? h.lits[b + i] : 0;
         }
     }
     bool ok = upload(&f->d_lits, h.lits.data(), h.lits.size()) && upload(&f->d_coff, coff.data(), coff.size()) &&

@@ -15,13 +15,14 @@
 //   formula (shared by all trails, read-only)
 //     lits[]   internal literals, CSR by clause
 //     w0off[]  per-var offsets into w0ent
-//     w0ent[]  int4 {clause, lit offset, length, (w1<<16)|w2} per initial watch,
-//              each var's entries in the reference's initial list order
+//     w0ent[]  32 bytes per initial watch: {clause, literal offset, length,
+//              (w1<<16)|w2} {first four literals}; each var's entries in the
+//              reference's initial list order
 //   per trail slot (one warp owns one slot; slots are reused across trails)
 //     asg[n]    uint8  (epoch<<1)|sign   trail + pending implications
 //     cst[m]    uint32 (epoch<<24)|(blocked<<22)|(w1<<11)|w2   clauses touched
 //     dh[n]     uint32 (epoch<<24)|arena index   head of clauses add_first'ed to a var
-//     arena[]   int4 {clause, lit offset, length, next}
+//     arena[]   32 bytes per entry: {clause, literal offset, length, next} {literals}
 //     stack[]   int2 depth-first frames (intervals of the implication list)
 //   A slot's epoch (1..127) advances per trail, so nothing is cleared between
 //   trails; the slot is wiped once every 127 trails.
@@ -32,18 +33,22 @@
 // false literals and nothing is unassigned within one BCP), so that is the
 // reference's linked list exactly.
 //
-// Execution: one warp per trail.  Each round gathers up to 32 upcoming watch
+// Execution: one warp per trail.  A round gathers up to 32 upcoming watch
 // entries -- the rest of the current scan and, while the current scan is a
 // trail scan that has implied nothing, the entries of the following trail
-// scans -- evaluates all of them at once against the current state, then
-// commits them in reference order, stopping before the first entry whose
-// evaluation an earlier entry of the round may have changed (same clause, or
-// a scan whose list an earlier switch extended) and right after the first
-// implication or conflict.  What is not committed is evaluated again next
-// round, so the result is the sequential one.
+// scans -- and evaluates all of them at once against the current state, with
+// every random load of the round (clause state, assignments, list heads) in
+// one trip.  It then commits them in reference order up to the first event
+// that could have changed a later evaluation: an entry whose clause an earlier
+// entry of the round already handled, a later scan whose list is not what the
+// round assumed (it has clauses add_first'ed to it, possibly by this round),
+// or the entry just after an implication or a conflict.  Events are encoded as
+// ordered keys and the cut is one warp min-reduction.  Uncommitted entries are
+// evaluated again next round, so the result is the sequential one.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 
 #include "internal.h"
@@ -53,7 +58,7 @@ namespace bcp {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int WARPS = 4;          // warps per block
-constexpr int KREG = 8;           // clause literals evaluated from registers
+constexpr int KIN = 4;            // clause literals stored inside a watch entry
 constexpr uint32_t EPMAX = 127;   // epochs per slot before a wipe
 constexpr int MAXLEN = 2048;      // clause length limit (11-bit watch indices)
 constexpr int64_t MAX_ITERS = int64_t(1) << 26;  // per-trail loop iterations before GPSAT_BCP_BUDGET
@@ -65,11 +70,11 @@ struct Dev {
     int32_t n_clauses;
     const int32_t *__restrict__ lits;
     const uint32_t *__restrict__ w0off;
-    const int4 *__restrict__ w0ent;
+    const int4 *__restrict__ w0ent;   // 2 int4 per entry
     uint8_t *asg;
     uint32_t *cst;
     uint32_t *dh;
-    int4 *arena;
+    int4 *arena;                      // 2 int4 per entry
     int2 *stack;
     uint32_t *epoch;
     unsigned int *next_trail;
@@ -85,7 +90,8 @@ struct Dev {
 };
 
 struct WarpSmem {
-    int4 ent[32];
+    int4 e0[32];
+    int4 e1[32];
     int32_t dp_after[32];
     int32_t sc_var[33];
     int32_t sc_begin[33];
@@ -106,12 +112,6 @@ __device__ __forceinline__ unsigned lanemask_gt()
     asm("mov.u32 %0, %%lanemask_gt;" : "=r"(r));
     return r;
 }
-__device__ __forceinline__ unsigned range_mask(int b, int e)
-{
-    unsigned hi = e >= 32 ? FULL : ((1u << e) - 1u);
-    unsigned lo = b >= 32 ? FULL : ((1u << b) - 1u);
-    return hi & ~lo;
-}
 template <class T>
 __device__ __forceinline__ T warp_sum(T x)
 {
@@ -121,7 +121,23 @@ __device__ __forceinline__ T warp_sum(T x)
 }
 __device__ __forceinline__ int32_t dimacs_of(int32_t l) { return (l & 1) ? (l >> 1) + 1 : -((l >> 1) + 1); }
 
-// consistency of literal l given its var's asg byte: unassigned in this epoch or true
+// position of the n-th set bit of m (n >= 1, m holds at least n set bits)
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (c < n) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+// literal l is consistent (unassigned in this epoch, or true) given its var's asg byte
 __device__ __forceinline__ bool cons_of(uint8_t a, int32_t l, uint32_t e)
 {
     return ((uint32_t)(a >> 1) != e) || ((a & 1) == (l & 1));
@@ -136,7 +152,8 @@ struct Eval {
     int acnt;           // assignment lookups as the reference counts them
 };
 
-// process_clause of the reference for one clause with watch indices w1, w2.
+// process_clause of the reference for a clause too long for the inline path
+// (literals read from the arena).
 __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const uint32_t *dh, int off, int len,
                                        int w1, int w2, uint32_t e, Eval &r)
 {
@@ -188,16 +205,22 @@ __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const u
     r.act = ((uint32_t)(asg[unit >> 1] >> 1) != e) ? A_IMPLY : A_BLOCK;
 }
 
+// commit-cut keys: (lane position << 7) | (window scan << 1) | after
+constexpr int NO_CUT = INT_MAX;
+__device__ __forceinline__ int key_before(int pos, int scan) { return (pos << 7) | (scan << 1); }
+__device__ __forceinline__ int key_after(int pos, int scan) { return ((pos + 1) << 7) | (scan << 1) | 1; }
+
 __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int lane)
 {
     uint8_t *asg = d.asg + (size_t)slot * d.n_pad;
     uint32_t *cst = d.cst + (size_t)slot * d.m_pad;
     uint32_t *dh = d.dh + (size_t)slot * d.n_pad;
-    int4 *arena = d.arena + (size_t)slot * d.arena_cap;
+    int4 *arena = d.arena + (size_t)slot * d.arena_cap * 2;
     int2 *stk = d.stack + (size_t)slot * d.impl_cap;
     int32_t *ilit = d.ilit + (size_t)t * d.impl_cap;
     int32_t *ireason = d.ireason + (size_t)t * d.impl_cap;
     const int32_t n = d.n_vars;
+    const unsigned lt = lanemask_lt();
 
     // ---- epoch of this slot
     uint32_t e = 0;
@@ -237,13 +260,19 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         bad = __any_sync(FULL, bad);
     }
 
-    int64_t n_impl = 0, props = 0, cW = 0, cL = 0, cA = 0, cI = 0;
+    int64_t n_impl = 0, props = 0, cI = 0;
+    int64_t myW = 0, myL = 0, myA = 0;  // lane-private, reduced at the end
     int32_t status = bad ? GPSAT_BCP_BAD_TRAIL : GPSAT_BCP_NO_CONFLICT, confl = -1, stopi = -1;
     int64_t arena_used = 0, ti = 0, top_j = 0, top_e = 0, cur_impl_start = 0, cur_trail = -1, dfs_trail = -1;
     int depth = 0;
     bool in_scan = false, cur_counted = false, cur_is_trail = false;
     int32_t cur_var = 0, cur_dp = -1;
     uint32_t cur_wk = 0, cur_wend = 0;
+    // look-ahead buffer: lane j holds trail position lb_base + j (its variable
+    // and initial watch-list range), refilled when fewer than 16 lie ahead
+    int64_t lb_base = INT64_MIN / 2;
+    int32_t lb_v = 0;
+    uint32_t lb_a = 0, lb_b = 0;
     // every iteration finishes a scan, pops a frame or commits at least one
     // entry; the budget only guarantees termination if that were ever broken
     int64_t budget = MAX_ITERS;
@@ -313,8 +342,9 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             if (lane == 0) {
                 int32_t p = cur_dp;
                 while (p >= 0 && ndyn < 32) {
-                    int4 a = arena[p];
-                    sm.ent[ndyn] = a;
+                    const int4 a = arena[2 * p];
+                    sm.e0[ndyn] = a;
+                    sm.e1[ndyn] = arena[2 * p + 1];
                     p = a.w;
                     sm.dp_after[ndyn] = p;
                     ndyn++;
@@ -328,7 +358,10 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         int take0 = 0;
         if (dyn_done) {
             take0 = min(32 - nent, (int)(cur_wend - cur_wk));
-            if (lane < take0) sm.ent[nent + lane] = d.w0ent[cur_wk + lane];
+            if (lane < take0) {
+                sm.e0[nent + lane] = d.w0ent[2 * (size_t)(cur_wk + lane)];
+                sm.e1[nent + lane] = d.w0ent[2 * (size_t)(cur_wk + lane) + 1];
+            }
             nent += take0;
         }
         if (lane == 0) {
@@ -337,31 +370,44 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             sm.sc_end[0] = nent;
         }
         int nsc = 1;
+        int my_scan = 0;
         const bool scan0_full = dyn_done && (cur_wk + (uint32_t)take0 == cur_wend);
         if (scan0_full && depth == 0 && cur_is_trail && n_impl == cur_impl_start && nent < 32 && ti < tn) {
+            // following trail scans, assumed to start with an empty added list
+            // (checked in the evaluation trip)
             const int room = 32 - nent;
-            const int nlook = (int)(tn - ti < 31 ? tn - ti : 31);
+            if (lb_base + 32 - ti < 16 && lb_base + 32 < tn) {
+                lb_base = ti;
+                if (ti + lane < tn) {
+                    const int32_t x = d.trail[tb + ti + lane];
+                    lb_v = (x > 0 ? x : -x) - 1;
+                    lb_a = d.w0off[lb_v];
+                    lb_b = d.w0off[lb_v + 1];
+                }
+            }
+            const int lb_off = (int)(ti - lb_base);
+            const int64_t ahead = (32 - lb_off < tn - ti) ? (int64_t)(32 - lb_off) : tn - ti;
+            const int nlook = (int)(ahead < 31 ? ahead : 31);
+            const int src = (lb_off + lane) & 31;
+            const int32_t bv = __shfl_sync(FULL, lb_v, src);
+            const uint32_t ba = __shfl_sync(FULL, lb_a, src), bb = __shfl_sync(FULL, lb_b, src);
             int32_t v = -1;
             uint32_t a = 0, b = 0;
-            bool dynne = false;
             if (lane < nlook) {
-                int32_t x = d.trail[tb + ti + lane];
-                v = (x > 0 ? x : -x) - 1;
-                uint32_t h = dh[v];
-                dynne = (h >> 24) == e;
-                a = d.w0off[v];
-                b = d.w0off[v + 1];
+                v = bv;
+                a = ba;
+                b = bb;
             }
-            int cnt = (lane < nlook) ? (int)(b - a < 32u ? b - a : 32u) : 0;
+            const int cnt = (lane < nlook) ? (int)(b - a < 32u ? b - a : 32u) : 0;
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 int y = __shfl_up_sync(FULL, incl, o);
                 if (lane >= o) incl += y;
             }
-            int excl = incl - cnt;
-            unsigned ok = __ballot_sync(FULL, lane < nlook && !dynne && excl < room);
-            int K = (~ok) ? __ffs(~ok) - 1 : 32;
+            const int excl = incl - cnt;
+            const unsigned ok = __ballot_sync(FULL, lane < nlook && excl < room);
+            const int K = (~ok) ? __ffs(~ok) - 1 : 32;
             if (lane < K) {
                 sm.sc_var[1 + lane] = v;
                 sm.sc_begin[1 + lane] = nent + excl;
@@ -370,17 +416,24 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 sm.sc_wend[1 + lane] = b;
             }
             if (K > 0) {
-                int total = nent + __shfl_sync(FULL, incl, K - 1);
-                total = min(total, 32);
-                int q = lane - nent;
-                int s = 0;
-                for (int j = 1; j < K; j++) {
-                    int ej = __shfl_sync(FULL, excl, j);
-                    if (q >= ej) s = j;
+                const int total = min(nent + __shfl_sync(FULL, incl, K - 1), 32);
+                // window position -> lookahead scan: rank among the scans that start
+                // at or before it, mapped through the mask of non-empty scans
+                const bool nonempty = lane < K && cnt > 0;
+                const unsigned nem = __ballot_sync(FULL, nonempty);
+                const unsigned starts = __reduce_or_sync(FULL, nonempty ? (1u << (nent + excl)) : 0u);
+                if (lane >= nent && lane < total) {
+                    const int rank = __popc(starts & (lane == 31 ? FULL : ((2u << lane) - 1u)));
+                    my_scan = 1 + nth_set_bit(nem, rank);
                 }
-                int es = __shfl_sync(FULL, excl, s);
-                uint32_t as = __shfl_sync(FULL, a, s);
-                if (lane >= nent && lane < total) sm.ent[lane] = d.w0ent[as + (uint32_t)(q - es)];
+                const int jj = my_scan - 1;
+                const int ej = __shfl_sync(FULL, excl, jj < 0 ? 0 : jj);
+                const uint32_t aj = __shfl_sync(FULL, a, jj < 0 ? 0 : jj);
+                if (lane >= nent && lane < total) {
+                    const size_t w = aj + (uint32_t)(lane - nent - ej);
+                    sm.e0[lane] = d.w0ent[2 * w];
+                    sm.e1[lane] = d.w0ent[2 * w + 1];
+                }
                 nent = total;
                 nsc = 1 + K;
             }
@@ -389,11 +442,12 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
 
         // ---- evaluate every entry of the window at once
         const bool has = lane < nent;
-        int my_scan = 0;
-        for (int s = 1; s < nsc; s++)
-            if (lane >= sm.sc_begin[s]) my_scan = s;
-        const int4 en = has ? sm.ent[lane] : make_int4(0, 0, 0, 0);
+        const int4 en = has ? sm.e0[lane] : make_int4(0, 0, 0, 0);
+        const int4 el = has ? sm.e1[lane] : make_int4(0, 0, 0, 0);
         const int32_t sv = sm.sc_var[my_scan];
+        // lane s (1 <= s < nsc) checks whether window scan s starts with added clauses
+        const int32_t scan_v = (lane >= 1 && lane < nsc) ? sm.sc_var[lane] : -1;
+        const int32_t scan_b = (lane >= 1 && lane < nsc) ? sm.sc_begin[lane] : 0;
         Eval r;
         r.act = A_NONE;
         r.acnt = 0;
@@ -403,9 +457,21 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         r.nw1 = r.nw2 = 0;
         bool valid = false;
         int w1 = 0, w2 = 0;
+        uint32_t scan_h = 0;
         if (has) {
             const uint32_t st = cst[en.x];
             const int len = en.z;
+            const int32_t Lr[KIN] = {el.x, el.y, el.z, el.w};
+            uint8_t Av[KIN];
+            uint32_t Dh[KIN];
+            // every random load of the round in one trip: clause state, the
+            // literals' assignments and list heads (unused ones are cheap misses)
+#pragma unroll
+            for (int i = 0; i < KIN; i++) {
+                Av[i] = (i < len) ? asg[Lr[i] >> 1] : 0;
+                Dh[i] = (i < len) ? dh[Lr[i] >> 1] : 0;
+            }
+            if (scan_v >= 0) scan_h = dh[scan_v];
             bool blk;
             if ((st >> 24) == e) {
                 blk = (st >> 22) & 1u;
@@ -416,31 +482,22 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 w1 = (uint32_t)en.w >> 16;
                 w2 = en.w & 0xFFFF;
             }
-            if (len <= KREG) {
-                int32_t Lr[KREG];
-#pragma unroll
-                for (int i = 0; i < KREG; i++) Lr[i] = (i < len) ? d.lits[en.y + i] : 0;  // pad: a valid index
+            if (len <= KIN) {
                 int32_t l1 = 0, l2 = 0;
+                bool c1 = false, c2 = false;
 #pragma unroll
-                for (int i = 0; i < KREG; i++) {
-                    if (i == w1) l1 = Lr[i];
-                    if (i == w2) l2 = Lr[i];
+                for (int i = 0; i < KIN; i++) {
+                    if (i == w1) {
+                        l1 = Lr[i];
+                        c1 = cons_of(Av[i], Lr[i], e);
+                    }
+                    if (i == w2) {
+                        l2 = Lr[i];
+                        c2 = cons_of(Av[i], Lr[i], e);
+                    }
                 }
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
                 if (valid) {
-                    uint8_t Av[KREG];
-                    uint32_t Dh[KREG];
-#pragma unroll
-                    for (int i = 0; i < KREG; i++) {
-                        Av[i] = (i < len) ? asg[Lr[i] >> 1] : 0;
-                        Dh[i] = (i < len && i != w1 && i != w2) ? dh[Lr[i] >> 1] : 0;
-                    }
-                    bool c1 = false, c2 = false;
-#pragma unroll
-                    for (int i = 0; i < KREG; i++) {
-                        if (i == w1) c1 = cons_of(Av[i], Lr[i], e);
-                        if (i == w2) c2 = cons_of(Av[i], Lr[i], e);
-                    }
                     r.acnt = 2;
                     if (!(c1 && c2)) {
                         int pend = (!c1 && !c2) ? 2 : 1, f1 = -1, f2 = -1;
@@ -448,7 +505,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                         uint32_t df1 = 0, df2 = 0;
                         uint8_t af1 = 0;
 #pragma unroll
-                        for (int i = 0; i < KREG; i++) {
+                        for (int i = 0; i < KIN; i++) {
                             if (i < len && pend > 0 && i != w1 && i != w2) {
                                 r.acnt++;
                                 if (cons_of(Av[i], Lr[i], e)) {
@@ -472,7 +529,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                             if (f1 < 0) {
                                 unit = c1 ? l1 : l2;
 #pragma unroll
-                                for (int i = 0; i < KREG; i++)
+                                for (int i = 0; i < KIN; i++)
                                     if (i == (c1 ? w1 : w2)) au = Av[i];
                             } else {
                                 r.act = A_SW1;
@@ -506,49 +563,41 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
                 if (valid) eval_long(d, asg, dh, en.y, len, w1, w2, e, r);
             }
+        } else if (scan_v >= 0) {
+            scan_h = dh[scan_v];
         }
 
-        // ---- commit in reference order
-        const unsigned lt = lanemask_lt();
-        const int key = has ? en.x : -1 - lane;
-        const unsigned mm = __match_any_sync(FULL, key);
-        const unsigned dupmask = __ballot_sync(FULL, has && (mm & lt) != 0);
-        const unsigned sammask = __ballot_sync(FULL, valid && (r.act == A_IMPLY || r.act == A_CONFLICT));
-        const bool isw = valid && (r.act == A_SW1 || r.act == A_SW2);
-        int k_end = nent, new_cur = 0;
-        bool new_started = true;
-        for (int s = 0; s < nsc; s++) {
-            const int b = sm.sc_begin[s], eo = sm.sc_end[s];
-            if (s >= 1) {
-                const int32_t vs = sm.sc_var[s];
-                unsigned hit = __ballot_sync(FULL, isw && lane < b && (r.t1 == vs || r.t2 == vs));
-                if (hit) {
-                    k_end = b;
-                    new_cur = s;
-                    new_started = false;
-                    break;
+        // ---- where the commit stops: the smallest event key of the round
+        int key = NO_CUT;
+        {
+            const int keyc = has ? en.x : -1 - lane;
+            const unsigned mm = __match_any_sync(FULL, keyc);
+            if (has && (mm & lt)) key = key_before(lane, my_scan);  // clause seen earlier this round
+            if (valid && (r.act == A_IMPLY || r.act == A_CONFLICT)) key = min(key, key_after(lane, my_scan));
+            // a later window scan whose list starts with added clauses
+            if (scan_v >= 0 && (scan_h >> 24) == e) key = min(key, key_before(scan_b, lane));
+            // a move of this lane that lands in a later window scan's list
+            if (valid && (r.act == A_SW1 || r.act == A_SW2)) {
+                for (int s = my_scan + 1; s < nsc; s++) {
+                    const int32_t vs = sm.sc_var[s];
+                    if (vs == r.t1 || vs == r.t2) {
+                        key = min(key, key_before(sm.sc_begin[s], s));
+                        break;
+                    }
                 }
             }
-            const unsigned rg = range_mask(b, eo);
-            const unsigned dm = dupmask & rg, smk = sammask & rg;
-            const int fd = dm ? __ffs(dm) - 1 : 32;
-            const int fs = smk ? __ffs(smk) - 1 : 32;
-            if (fd < 32 || fs < 32) {
-                new_cur = s;
-                if (fd <= fs) {
-                    k_end = fd;
-                    new_started = (s == 0) || (fd > b);
-                } else {
-                    k_end = fs + 1;
-                    new_started = true;
-                }
-                break;
-            }
-            if (s == nsc - 1) {
-                k_end = eo;
-                new_cur = s;
-                new_started = (s == 0) || (eo > b);
-            }
+        }
+        const int cut = __reduce_min_sync(FULL, key);
+        int k_end, new_cur;
+        bool new_started;
+        if (cut == NO_CUT) {
+            k_end = nent;
+            new_cur = nsc - 1;
+            new_started = (new_cur == 0) || (sm.sc_end[new_cur] > sm.sc_begin[new_cur]);
+        } else {
+            k_end = cut >> 7;
+            new_cur = (cut >> 1) & 63;
+            new_started = (cut & 1) || new_cur == 0 || k_end > sm.sc_begin[new_cur];
         }
 
         const bool com = valid && lane < k_end;
@@ -558,14 +607,17 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         const unsigned m1 = __ballot_sync(FULL, ins1), m2 = __ballot_sync(FULL, ins2);
         const int total_ins = __popc(m1) + __popc(m2);
         if (arena_used + total_ins > d.arena_cap) {
+            const int ks = __shfl_sync(FULL, my_scan, __ffs(m1) - 1);
             status = GPSAT_BCP_OVERFLOW;
-            stopi = (int32_t)cur_trail;
+            stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
             break;
         }
         const unsigned imask = __ballot_sync(FULL, com && r.act == A_IMPLY);
         if (imask && n_impl >= d.impl_cap) {
+            // stop index: the trail literal whose propagation overflowed
+            const int ks = __shfl_sync(FULL, my_scan, __ffs(imask) - 1);
             status = GPSAT_BCP_OVERFLOW;
-            stopi = (int32_t)cur_trail;
+            stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
             break;
         }
         if (m2 == 0) {
@@ -580,7 +632,8 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 } else {
                     next = ((r.dh1 >> 24) == e) ? (int32_t)(r.dh1 & 0xFFFFFFu) : -1;
                 }
-                arena[myidx] = make_int4(en.x, en.y, en.z, next);
+                arena[2 * myidx] = make_int4(en.x, en.y, en.z, next);
+                arena[2 * myidx + 1] = el;
                 if ((g & lanemask_gt()) == 0) dh[r.t1] = (e << 24) | (uint32_t)myidx;
             }
         } else {
@@ -593,17 +646,21 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 rem &= rem - 1;
                 const int32_t c = __shfl_sync(FULL, en.x, k), off = __shfl_sync(FULL, en.y, k),
                               len = __shfl_sync(FULL, en.z, k);
+                const int4 lk = make_int4(__shfl_sync(FULL, el.x, k), __shfl_sync(FULL, el.y, k),
+                                          __shfl_sync(FULL, el.z, k), __shfl_sync(FULL, el.w, k));
                 const int32_t tt1 = __shfl_sync(FULL, r.t1, k), tt2 = __shfl_sync(FULL, r.t2, k);
                 const bool two = (m2 >> k) & 1u;
                 if (lane == 0) {
                     uint32_t h = dh[tt1];
                     int32_t next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-                    arena[idx] = make_int4(c, off, len, next);
+                    arena[2 * idx] = make_int4(c, off, len, next);
+                    arena[2 * idx + 1] = lk;
                     dh[tt1] = (e << 24) | (uint32_t)idx;
                     if (two) {
                         h = dh[tt2];
                         next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-                        arena[idx + 1] = make_int4(c, off, len, next);
+                        arena[2 * (idx + 1)] = make_int4(c, off, len, next);
+                        arena[2 * (idx + 1) + 1] = lk;
                         dh[tt2] = (e << 24) | (uint32_t)(idx + 1);
                     }
                 }
@@ -631,9 +688,11 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             cI++;
         }
         const unsigned cmask = __ballot_sync(FULL, com && r.act == A_CONFLICT);
-        cW += __popc(__ballot_sync(FULL, com));
-        cL += warp_sum(com ? en.z : 0);
-        cA += warp_sum(com ? r.acnt : 0);
+        if (com) {
+            myW++;
+            myL += en.z;
+            myA += r.acnt;
+        }
         const int64_t ti_round = ti;
         __syncwarp();
 
@@ -651,6 +710,12 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             props += new_cur - 1;
             cur_var = sm.sc_var[new_cur];
             cur_dp = -1;
+            if (!new_started) {
+                // cut before this scan because its list starts with added
+                // clauses (possibly added by this round): those come first
+                const uint32_t h = dh[cur_var];
+                cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+            }
             cur_wk = sm.sc_wk[new_cur] + (uint32_t)(k_end - sm.sc_begin[new_cur]);
             cur_wend = sm.sc_wend[new_cur];
             cur_counted = new_started;
@@ -671,6 +736,9 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         __syncwarp();
     }
 
+    myW = warp_sum(myW);
+    myL = warp_sum(myL);
+    myA = warp_sum(myA);
     if (lane == 0) {
         d.status[t] = status;
         d.conflict[t] = confl;
@@ -679,16 +747,20 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         if (d.counters) {
             int64_t *cn = d.counters + (size_t)t * GPSAT_BCP_NCOUNTERS;
             cn[0] = props;
-            cn[1] = cW;
-            cn[2] = cL;
-            cn[3] = cA;
+            cn[1] = myW;
+            cn[2] = myL;
+            cn[3] = myA;
             cn[4] = cI;
             cn[5] = bad ? 0 : tn;
         }
     }
 }
 
-__global__ void __launch_bounds__(WARPS * 32, 8) bcp_kernel(Dev d)
+// blocks per SM the register allocation targets (8 = 32 resident warps per SM)
+#ifndef GPSAT_BCP_MIN_BLOCKS
+#define GPSAT_BCP_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(WARPS * 32, GPSAT_BCP_MIN_BLOCKS) bcp_kernel(Dev d)
 {
     __shared__ WarpSmem smem[WARPS];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -815,7 +887,7 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
     b->m_pad = (f->h.n_clauses() + 3) / 4 * 4;
     b->impl_cap = impl_cap;
     b->arena_cap = arena_cap ? arena_cap : (1 << 17);
-    const int64_t per_slot = b->n_pad * 5 + b->m_pad * 4 + b->arena_cap * 16 + b->impl_cap * 8;
+    const int64_t per_slot = b->n_pad * 5 + b->m_pad * 4 + b->arena_cap * 32 + b->impl_cap * 8;
     int32_t slots = max_slots ? max_slots : resident;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -827,7 +899,7 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
               cudaMalloc(&b->cst, S * b->m_pad * 4) == cudaSuccess &&
               cudaMalloc(&b->dh, S * b->n_pad * 4) == cudaSuccess &&
               cudaMalloc(&b->epoch, S * 4) == cudaSuccess &&
-              cudaMalloc(&b->arena, S * b->arena_cap * 16) == cudaSuccess &&
+              cudaMalloc(&b->arena, S * b->arena_cap * 32) == cudaSuccess &&
               cudaMalloc(&b->stack, S * b->impl_cap * 8) == cudaSuccess &&
               cudaMalloc(&b->counter, 16) == cudaSuccess;
     if (ok)

@@ -131,6 +131,84 @@ int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *t
 /* Trails in flight and the device bytes the workspace holds. */
 int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
 
+/* ---- CDCL solving on the device -------------------------------------------
+ * One warp runs one complete CDCL search (two watched literals, first-UIP
+ * learning, VSIDS, restarts) for one job; a persistent grid pulls jobs from a
+ * global counter.  A job is a whole formula or a formula restricted to a cube
+ * of assumption literals (the reference's JobChooser jobs).  Replaces the
+ * reference's sequential kernel run_sequential and the relaunched
+ * parallel_kernel (SATSolver/Parallelizer.cu:133-277, main.cu:197-310). */
+#define GPSAT_DECIDE_VSIDS 0      /* DecisionStrategy: VSIDS (reference DecisionStrategy/VSIDS.cu) */
+#define GPSAT_DECIDE_LAST_FREE 1  /* the reference's default rule (SATSolver/DecisionMaker.cu:45-55) */
+#define GPSAT_RESTART_NONE 0
+#define GPSAT_RESTART_LUBY 1
+#define GPSAT_RESTART_GEOMETRIC 2 /* reference Restarts/GeometricRestartsManager.cu (100, x1.3) */
+
+typedef struct {
+    int32_t decide;            /* GPSAT_DECIDE_* */
+    int32_t restart;           /* GPSAT_RESTART_* */
+    int32_t restart_base;      /* conflicts: Luby unit or first geometric interval */
+    float restart_factor;      /* geometric growth */
+    float var_decay;           /* VSIDS activity decay per conflict */
+    int32_t learnt_first;      /* ClauseLearning: learnt clauses kept before the first reduction */
+    int32_t learnt_inc;        /* growth of that limit per reduction */
+    int32_t minimize;          /* ConflictAnalysis: basic learnt-clause minimisation */
+    int64_t conflict_budget;   /* per job; reaching it ends the job UNKNOWN (0 = none) */
+    int32_t phase_init;        /* first polarity of an unseeded variable: 0 false, 1 true */
+    int32_t max_slots;         /* jobs in flight (0 = as many as the GPU keeps resident) */
+    int32_t log_participation; /* count, per variable, the conflicts whose analysis saw it */
+    int32_t reserved[5];
+} gpsat_solve_options;
+
+/* per-formula statistics written by gpsat_batch_solve (summed over its jobs) */
+#define GPSAT_SOLVE_NSTATS 9
+/* [0] conflicts [1] decisions [2] propagations [3] restarts [4] learnt clauses
+ * kept [5] reductions [6] watch rebuilds [7] flags (1 cancelled, 2 slot too
+ * small, 4 conflict budget) [8] jobs                                        */
+
+int gpsat_solve_options_default(gpsat_solve_options *o);
+
+typedef struct gpsat_batch gpsat_batch;
+/* Formulas f = 0..n_formulas-1: clauses formula_offsets[f] .. formula_offsets[f+1]
+ * of the CSR (lits, clause_offsets); n_vars[f] variables each.  Every formula
+ * goes through the reference's preprocessing on the host, then is uploaded. */
+int gpsat_batch_create(const int32_t *lits, const int64_t *clause_offsets, const int64_t *formula_offsets,
+                       const int32_t *n_vars, int32_t n_formulas, gpsat_batch **out);
+int gpsat_batch_destroy(gpsat_batch *b);
+int gpsat_batch_info(const gpsat_batch *b, int32_t *n_formulas, int64_t *total_vars, int32_t *slots,
+                     int64_t *workspace_bytes);
+/* Optional per-variable seeds (concatenated over formulas, NULL to clear):
+ * initial VSIDS activity and initial phase (0 false, 1 true). */
+int gpsat_batch_set_seeds(gpsat_batch *b, const float *activity, const int8_t *phase);
+/* Solves every formula.  Jobs: job_formula[j] with cube literals
+ * cube_lits[cube_offsets[j] .. cube_offsets[j+1]) (DIMACS); job_formula NULL =
+ * one job per formula.  A formula is SAT when one of its jobs finds a model
+ * (the other jobs of it are cancelled), UNSAT when all its jobs are refuted,
+ * otherwise UNKNOWN.  Outputs per formula: verdicts, models (n_vars bytes each,
+ * +1 true / -1 false, concatenated; may be NULL), stats (GPSAT_SOLVE_NSTATS
+ * each; may be NULL), model_ok (device checker: 1 every original clause holds
+ * a true literal, 0 not, -1 no model; may be NULL), participation (int32 per
+ * variable, with log_participation; may be NULL). */
+int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt, const int32_t *job_formula,
+                      const int64_t *cube_offsets, const int32_t *cube_lits, int32_t n_jobs, int32_t *verdicts,
+                      int8_t *models, int64_t *stats, int32_t *model_ok, int32_t *participation);
+/* Independent host model check: 1 if every clause holds a true literal, 0 if
+ * not (first_false_clause set), negative on bad input.
+ * (the reference's own "verified" check, SATSolver/Results.cu:143-155,
+ *  ignores literal signs; this one does not) */
+int gpsat_check_model(const int32_t *lits, const int64_t *offsets, int64_t n_clauses, const int8_t *model,
+                      int32_t n_vars, int64_t *first_false_clause);
+
+/* ---- DIMACS input (host) ---------------------------------------------------
+ * Parses CNF text.  Call once with lits/offsets NULL for the sizes, then with
+ * buffers of n_lits and n_clauses+1 entries.  n_vars is the highest variable
+ * that occurs, as the reference's reader sets it; the header's counts are
+ * returned for comparison.  Malformed text gives GPSAT_ERR_PARSE with the
+ * line in gpsat_last_error().  (replaces CnfManager::read_cnf, reference
+ * FileManager/CnfReader.cpp:30-135) */
+int gpsat_dimacs_parse(const char *text, int64_t len, int32_t *n_vars, int64_t *n_clauses, int64_t *n_lits,
+                       int32_t *header_vars, int64_t *header_clauses, int32_t *lits, int64_t *offsets);
+
 /* ---- seeded synthetic inputs (host) ---------------------------------------
  * Generator: splitmix64, one independent stream per clause / per trail, so
  * outputs do not depend on thread count.  uniform(n) = high 64 bits of

@@ -12,13 +12,14 @@ library never does.
 from __future__ import annotations
 
 import ctypes
+import platform
 import subprocess
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-LIB = HERE / "liboracle.so"
+LIB = HERE / f"liboracle_{platform.machine()}.so"
 SOURCES = [HERE / "bcp_ref.c"]
 
 _lib = None

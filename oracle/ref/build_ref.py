@@ -3,8 +3,8 @@
 Test infrastructure only.  Output goes to oracle/_ref/ (git-ignored):
 
   oracle/_ref/src_<variant>/   build-dir copy of the reference's src/ tree
-  oracle/_ref/obj_<variant>/   objects
-  oracle/_ref/libref_<variant>.so
+  oracle/_ref/obj_<variant>_<arch>/   objects
+  oracle/_ref/libref_<variant>_<arch>.so
       stock  -- Configs.cuh as shipped (MAX_ITERATIONS 1000)
       nocap  -- MAX_ITERATIONS raised to 2e9 in the copy, nothing else changed
 
@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -101,11 +102,11 @@ def _compile(args):
 
 
 def build_variant(variant: str) -> Path:
-    lib = OUT / f"libref_{variant}.so"
+    lib = OUT / f"libref_{variant}_{platform.machine()}.so"
     if lib.exists():
         return lib
     src = _prepare_copy(variant)
-    obj = OUT / f"obj_{variant}"
+    obj = OUT / f"obj_{variant}_{platform.machine()}"
     obj.mkdir(parents=True, exist_ok=True)
     base = ["g++", "-std=c++20", "-O2", "-fPIC", "-DNDEBUG", "-w", "-x", "c++", "-I", str(SHIM), "-I", str(src),
             "-include", "cuda_shim_pre.h"]

@@ -40,7 +40,11 @@ def test_bcp_matches_oracle_random(gpsat, orc, cuda_ok, n, ratio, k, T, fmin, fm
     tl, to = gpsat.gen_trails(seed + 77, n, T, fmin, fmax)
     g, o = run_both(gpsat, orc, lits, off, n, tl, to, impl_cap=n)
     compare_bcp(g, o, label=f"n={n} k={k}")
-    assert np.array_equal(g["counters"], o["counters"])
+    bad = np.nonzero((g["counters"] != o["counters"]).any(1))[0]
+    assert len(bad) == 0, (f"counters differ on {len(bad)} trails, first {bad[:5].tolist()}: gpu "
+                           f"{g['counters'][bad[:3]].tolist()} oracle {o['counters'][bad[:3]].tolist()} "
+                           f"status {g['status'][bad[:3]].tolist()} n_impl {g['n_impl'][bad[:3]].tolist()} "
+                           f"len {(to[bad[:3] + 1] - to[bad[:3]]).tolist()}")
     assert (g["status"] == 1).any() and (g["status"] == 0).any() or T < 300
 
 
@@ -87,7 +91,12 @@ def test_bcp_capacity_overflow_is_reported(gpsat, orc, cuda_ok):
     assert (g["status"] == -1).any()
     f = gpsat.Formula(lits, off, n)
     g2 = gpsat.BCPBatch(f, impl_cap=n, arena_cap=2).run_host(tl, to)
-    assert (g2["status"] == -1).all()
+    over = g2["status"] == -1
+    assert over.mean() > 0.8
+    # trails that finished inside the tiny move arena are still exact
+    o2 = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=n)
+    compare_bcp({k: v[~over] for k, v in g2.items() if v is not None}, o2, trails=list(np.nonzero(~over)[0]),
+                label="arena cap")
 
 
 def test_bcp_device_entry_matches_host_entry(gpsat, cuda_ok):
