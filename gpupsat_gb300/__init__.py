@@ -88,6 +88,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_gen_random_ksat": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]),
         "gpsat_gen_trails": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                             ctypes.c_double, _vp, _vp]),
+        "gpsat_gen_planted": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_double, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -127,6 +129,15 @@ def gen_random_ksat(seed: int, n_vars: int, n_clauses: int, k: int = 3) -> tuple
     lits = np.empty(n_clauses * k, dtype=np.int32)
     check(lib().gpsat_gen_random_ksat(seed, n_vars, n_clauses, k, _p(lits)))
     return lits, np.arange(0, n_clauses * k + 1, k, dtype=np.int64)
+
+
+def gen_planted(seed: int, n_vars: int, n_clauses: int, k: int = 3, communities: int = 40, p_in: float = 0.9):
+    """Planted k-SAT with community structure. Returns (lits, offsets, planted)
+    where planted[v-1] = +1/-1 is the hidden satisfying assignment."""
+    lits = np.empty(n_clauses * k, dtype=np.int32)
+    planted = np.empty(n_vars, dtype=np.int8)
+    check(lib().gpsat_gen_planted(seed, n_vars, n_clauses, k, communities, p_in, _p(lits), _p(planted)))
+    return lits, np.arange(0, n_clauses * k + 1, k, dtype=np.int64), planted
 
 
 def gen_trails(seed: int, n_vars: int, n_trails: int, fmin: float = 0.01, fmax: float = 0.05):

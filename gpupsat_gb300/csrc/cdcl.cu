@@ -769,6 +769,16 @@ __device__ __forceinline__ double luby(double y, int x)
     return r;
 }
 
+// Whether another job already found a model for the instance.  Another warp
+// may set the flag at any time, so lane 0 reads it once for the whole warp:
+// the answer guards warp-collective code and must be warp-uniform.
+__device__ __forceinline__ bool instance_closed(const Params &P, int inst)
+{
+    int v = 0;
+    if ((threadIdx.x & 31) == 0) v = *(volatile int32_t *)&P.inst_state[inst];
+    return __shfl_sync(FULL, v, 0) != 0;
+}
+
 // ---------------------------------------------------------------- one job
 __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *stats)
 {
@@ -903,8 +913,7 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
                 result = R_UNKNOWN;
                 break;
             }
-            if (o.check_every > 0 && (C.conflicts % o.check_every) == 0 &&
-                *(volatile int32_t *)&P.inst_state[inst] != 0) {
+            if (o.check_every > 0 && (C.conflicts % o.check_every) == 0 && instance_closed(P, inst)) {
                 stats[ST_FLAGS] |= FL_CANCELLED;
                 result = R_UNKNOWN;
                 break;
@@ -998,7 +1007,7 @@ __global__ void __launch_bounds__(WARPS * 32) cdcl_kernel(Params P)
         int64_t st[NSTATS];
         for (int i = 0; i < NSTATS; i++) st[i] = 0;
         int res = R_UNKNOWN;
-        if (*(volatile int32_t *)&P.inst_state[inst] != 0) {
+        if (instance_closed(P, inst)) {
             st[ST_FLAGS] |= FL_CANCELLED;
         } else {
             res = solve_job(P, C, job, inst, st);

@@ -1,4 +1,5 @@
-// Seeded synthetic inputs: uniform random k-SAT and random partial trails.
+// Seeded synthetic inputs: uniform random k-SAT, planted k-SAT with community
+// structure, and random partial trails.
 //
 // Generator: splitmix64 with one independent stream per clause or per trail
 // (stream state = mix(seed, index)), so the output is the same whatever the
@@ -115,6 +116,54 @@ extern "C" int gpsat_gen_trails(uint64_t seed, int32_t n_vars, int32_t n_trails,
                 int32_t v = out[i];
                 bits[(uint32_t)v >> 6] = 0;
                 out[i] = (r.next() >> 63) ? v + 1 : -(v + 1);
+            }
+        }
+    });
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_gen_planted(uint64_t seed, int32_t n_vars, int64_t n_clauses, int32_t k, int32_t n_communities,
+                                 double p_in, int32_t *lits, int8_t *planted)
+{
+    if (n_vars <= 0 || n_clauses < 0 || k <= 0 || k > 64 || n_communities <= 0 || n_communities > n_vars ||
+        k > n_vars / n_communities || !(p_in >= 0.0 && p_in <= 1.0) || (n_clauses > 0 && !lits))
+        return set_error(GPSAT_ERR_ARG,
+                         "gpsat_gen_planted: need 0 < k <= n_vars / n_communities, k <= 64, 0 <= p_in <= 1");
+    // the hidden assignment: one bit per variable from its own stream
+    auto value = [&](int32_t v) { return (Rng(seed, 0x504C414E00000000ULL + (uint64_t)v).next() >> 63) != 0; };
+    if (planted)
+        parallel_for(n_vars, [&](int64_t b, int64_t e, int) {
+            for (int64_t v = b; v < e; v++) planted[v] = value((int32_t)v) ? 1 : -1;
+        });
+    // community g holds variables [g*n/G, (g+1)*n/G)
+    auto first = [&](int64_t g) { return (int32_t)(g * n_vars / n_communities); };
+    parallel_for(n_clauses, [&](int64_t b, int64_t e, int) {
+        for (int64_t c = b; c < e; c++) {
+            Rng r(seed, (uint64_t)c);
+            int32_t *out = lits + c * k;
+            const int32_t g = (int32_t)r.below((uint32_t)n_communities);
+            const int32_t lo = first(g), size = first(g + 1) - lo;
+            for (int32_t i = 0; i < k; i++) {
+                const bool inside = r.unit() < p_in;
+                uint32_t v;
+                bool dup;
+                do {
+                    v = inside ? (uint32_t)lo + r.below((uint32_t)size) : r.below((uint32_t)n_vars);
+                    dup = false;
+                    for (int32_t j = 0; j < i; j++) dup |= (uint32_t)(std::abs(out[j]) - 1) == v;
+                } while (dup);
+                out[i] = (int32_t)v + 1;
+            }
+            // signs: uniform over the patterns the hidden assignment satisfies
+            // (rejection: a pattern is redrawn while every literal is false)
+            bool sat = false;
+            while (!sat) {
+                for (int32_t i = 0; i < k; i++) {
+                    const int32_t v = std::abs(out[i]);
+                    const bool pos = (r.next() >> 63) != 0;
+                    out[i] = pos ? v : -v;
+                    sat |= pos == value(v - 1);
+                }
             }
         }
     });

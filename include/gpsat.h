@@ -222,6 +222,16 @@ int gpsat_gen_random_ksat(uint64_t seed, int32_t n_vars, int64_t n_clauses, int3
  * Call with lits == NULL to get offsets (n_trails+1 entries) only. */
 int gpsat_gen_trails(uint64_t seed, int32_t n_vars, int32_t n_trails, double fmin,
                      double fmax, int64_t *offsets, int32_t *lits);
+/* Planted k-SAT with community structure: the variables form n_communities
+ * equal contiguous blocks; clause c picks a block uniformly and each of its
+ * k distinct variables comes from that block with probability p_in, else
+ * from all variables.  A hidden assignment (planted[v] = +1/-1, optional
+ * output) satisfies every clause: signs are drawn uniformly among the
+ * patterns it satisfies.  lits holds m*k ints as in gpsat_gen_random_ksat.
+ * (no counterpart in the reference, which reads CNF files only: this is the
+ * structured-batch workload's generator) */
+int gpsat_gen_planted(uint64_t seed, int32_t n_vars, int64_t n_clauses, int32_t k,
+                      int32_t n_communities, double p_in, int32_t *lits, int8_t *planted);
 
 #ifdef __cplusplus
 }

@@ -72,6 +72,26 @@ def test_generators_are_seeded_and_valid(gpsat):
         assert len(np.unique(v)) == len(v) and v.min() >= 1 and v.max() <= 1000
 
 
+def test_planted_generator(gpsat):
+    n, m, G = 4000, 16000, 40
+    lits, off, planted = gpsat.gen_planted(3, n, m, 3, G, 0.9)
+    lits2, _, planted2 = gpsat.gen_planted(3, n, m, 3, G, 0.9)
+    assert np.array_equal(lits, lits2) and np.array_equal(planted, planted2)
+    cl = lits.reshape(-1, 3)
+    v = np.abs(cl)
+    assert v.min() >= 1 and v.max() <= n and (np.sort(v, 1)[:, 1:] != np.sort(v, 1)[:, :-1]).all()
+    # the hidden assignment satisfies every clause
+    assert ((np.sign(cl) == planted[v - 1]).any(1)).all()
+    assert 0.3 < (planted > 0).mean() < 0.7
+    # most literals share their clause's majority community
+    comm = (v - 1) * G // n
+    major = np.array([np.bincount(r, minlength=G).max() for r in comm])
+    assert (major >= 2).mean() > 0.9
+    assert gpsat.check_model(lits, off, planted, n)
+    with pytest.raises(gpsat.GpsatError):
+        gpsat.gen_planted(1, 50, 10, 3, 40, 0.9)   # communities of one variable cannot hold 3
+
+
 def test_bcp_without_device_fails_loudly(gpsat):
     if gpsat.device_count() > 0:
         pytest.skip("a GPU is visible; covered by the GPU tests")
