@@ -77,6 +77,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_bcp_info": (ctypes.c_int, [_vp, _c_i32p, _c_i64p]),
         "gpsat_bcp_run_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 8),
         "gpsat_bcp_run_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 7),
+        "gpsat_bcp_run_static": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp, ctypes.c_int32]
+                                 + [_vp] * 8),
         "gpsat_solve_options_default": (ctypes.c_int, [ctypes.POINTER(SolveOptions)]),
         "gpsat_batch_create": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
         "gpsat_batch_destroy": (ctypes.c_int, [_vp]),
@@ -252,6 +254,18 @@ class BCPBatch:
             self.close()
         except Exception:
             pass
+
+
+def bcp_run_static(formula: Formula, trail_lits, trail_offsets, out: dict, impl_cap: int, arena_cap: int = 0,
+                   stream: int | None = None) -> None:
+    """gpsat_bcp_run_static: BCP with the library's fixed device scratch (no
+    allocation inside the call).  Device buffers (torch tensors) as in
+    BCPBatch.run_device; the formula must already be on the device (creating
+    a BCPBatch on it uploads it)."""
+    T = trail_offsets.numel() - 1
+    check(lib().gpsat_bcp_run_static(formula.handle, impl_cap, arena_cap, _p(trail_lits), _p(trail_offsets), T,
+                                     _p(out["status"]), _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
+                                     _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out.get("counters")), stream))
 
 
 # ---------------------------------------------------------------- CDCL solving

@@ -50,6 +50,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <mutex>
 
 #include "internal.h"
 
@@ -1034,5 +1035,185 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
                           cudaMemcpyDeviceToHost) == cudaSuccess;
     }
     if (!ok) return cuda_error(cudaGetLastError(), "implication copy");
+    return GPSAT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry: the per-trail state in a fixed device array
+// ---------------------------------------------------------------------------
+// For callers that cannot allocate device memory while they propagate: code
+// that captures the call into a CUDA graph (no cudaMalloc/cudaFree on a
+// capturing stream, and a replayed graph needs addresses that do not move)
+// and hosts whose device memory is reserved up front by their own pool.  The
+// call below makes no allocating CUDA call and no library allocation; the
+// slots' state lives in bcp_static_scratch, laid out afresh by every call:
+//   [launch counter | epoch per slot | asg | cst | dh | move arena | stack]
+// each part 256-byte aligned.  Everything but the arena and the stack (which
+// the kernel writes before it reads) is cleared on the stream per call.  One
+// array per device, so calls whose GPU work overlaps race on it.
+namespace gpsat {
+namespace bcp {
+
+static __device__ __align__(256) unsigned char bcp_static_scratch[GPSAT_BCP_STATIC_SCRATCH_BYTES];
+
+}  // namespace bcp
+}  // namespace gpsat
+
+namespace {
+
+constexpr int STATIC_MAX_DEVICES = 64;
+constexpr int64_t STATIC_ALIGN = 256;
+
+inline int64_t align_up(int64_t x) { return (x + STATIC_ALIGN - 1) / STATIC_ALIGN * STATIC_ALIGN; }
+
+struct StaticScratch {
+    std::mutex mu;
+    bool ready[STATIC_MAX_DEVICES] = {};
+    unsigned char *base[STATIC_MAX_DEVICES] = {};
+    int32_t resident[STATIC_MAX_DEVICES] = {};
+};
+
+StaticScratch &static_scratch()
+{
+    static StaticScratch s;
+    return s;
+}
+
+// Once per device, with that device current: the array's device address and
+// the resident warp count of the BCP kernel.  The lookup may load the module,
+// which is why the first call must not come inside a stream capture.
+int static_setup(int device, unsigned char **base, int32_t *resident)
+{
+    if (device < 0 || device >= STATIC_MAX_DEVICES)
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_static: device ordinal out of range");
+    StaticScratch &s = static_scratch();
+    std::lock_guard<std::mutex> lock(s.mu);
+    if (!s.ready[device]) {
+        void *ptr = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&ptr, bcp::bcp_static_scratch);
+        if (err != cudaSuccess) return cuda_error(err, "cudaGetSymbolAddress(bcp_static_scratch)");
+        int sms = 0, per_sm = 0;
+        err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (err != cudaSuccess) return cuda_error(err, "cudaDeviceGetAttribute");
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::WARPS * 32, 0);
+        if (err != cudaSuccess) return cuda_error(err, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        s.base[device] = static_cast<unsigned char *>(ptr);
+        s.resident[device] = std::max(1, sms * std::max(per_sm, 1) * bcp::WARPS);
+        s.ready[device] = true;
+    }
+    *base = s.base[device];
+    *resident = s.resident[device];
+    return GPSAT_OK;
+}
+
+// Bytes of the scratch layout for S slots (each part rounded up to 256).
+int64_t static_layout_bytes(int64_t S, int64_t n_pad, int64_t m_pad, int64_t arena_cap, int64_t impl_cap)
+{
+    return STATIC_ALIGN + align_up(S * 4) + align_up(S * n_pad) + align_up(S * m_pad * 4) +
+           align_up(S * n_pad * 4) + align_up(S * arena_cap * 32) + align_up(S * impl_cap * 8);
+}
+
+}  // namespace
+
+extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, int64_t arena_cap,
+                                    const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails,
+                                    int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                                    int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters,
+                                    void *stream)
+{
+    if (!f || impl_cap <= 0 || impl_cap > INT32_MAX || arena_cap < 0 || arena_cap > (1 << 24) || n_trails < 0 ||
+        (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index || !n_impl || !impl_lit ||
+                          !impl_reason)))
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_static: bad argument");
+    if (f->h.verdict != GPSAT_UNKNOWN)
+        return set_error(GPSAT_ERR_STATE, "formula was decided by preprocessing; nothing to propagate");
+    if (f->h.max_len > bcp::MAXLEN) return set_error(GPSAT_ERR_CAPACITY, "clause longer than 2048 literals");
+    if (!f->uploaded)
+        return set_error(GPSAT_ERR_STATE,
+                         "gpsat_bcp_run_static: the formula is not on the device yet (gpsat_bcp_create on it "
+                         "uploads it; this entry point allocates nothing, so it cannot upload)");
+    cudaError_t err = cudaSetDevice(f->device);
+    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    unsigned char *base = nullptr;
+    int32_t resident = 0;
+    int rc = static_setup(f->device, &base, &resident);
+    if (rc != GPSAT_OK) return rc;
+
+    const int64_t n_pad = ((int64_t)f->h.n_vars + 15) / 16 * 16;
+    const int64_t m_pad = (f->h.n_clauses() + 3) / 4 * 4;
+    const int64_t acap = arena_cap ? arena_cap : (1 << 17);
+    const int64_t limit = GPSAT_BCP_STATIC_SCRATCH_BYTES;
+    if (static_layout_bytes(1, n_pad, m_pad, acap, impl_cap) > limit) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "gpsat_bcp_run_static: one trail's state needs %lld bytes (n_vars %d, %lld clauses, "
+                      "arena_cap %lld, impl_cap %lld) but the static scratch holds %lld bytes",
+                      (long long)static_layout_bytes(1, n_pad, m_pad, acap, impl_cap), f->h.n_vars,
+                      (long long)f->h.n_clauses(), (long long)acap, (long long)impl_cap, (long long)limit);
+        return set_error(GPSAT_ERR_CAPACITY, msg);
+    }
+    int64_t S = std::min<int64_t>(resident, std::max<int32_t>(n_trails, 1));
+    const int64_t per_slot = 4 + n_pad * 5 + m_pad * 4 + acap * 32 + impl_cap * 8;
+    S = std::min<int64_t>(S, std::max<int64_t>(1, (limit - 7 * STATIC_ALIGN) / per_slot));
+    while (S > 1 && static_layout_bytes(S, n_pad, m_pad, acap, impl_cap) > limit) S--;
+
+    unsigned char *p = base;
+    auto take = [&](int64_t bytes) {
+        unsigned char *q = p;
+        p += align_up(bytes);
+        return q;
+    };
+    unsigned int *counter = reinterpret_cast<unsigned int *>(take(STATIC_ALIGN));
+    uint32_t *epoch = reinterpret_cast<uint32_t *>(take(S * 4));
+    uint8_t *asg = take(S * n_pad);
+    uint32_t *cst = reinterpret_cast<uint32_t *>(take(S * m_pad * 4));
+    uint32_t *dh = reinterpret_cast<uint32_t *>(take(S * n_pad * 4));
+    int4 *arena = reinterpret_cast<int4 *>(take(S * acap * 32));
+    int2 *stack = reinterpret_cast<int2 *>(take(S * impl_cap * 8));
+
+    cudaStream_t st = (cudaStream_t)stream;
+    // what the kernel expects to find zero: the launch counter, the slots'
+    // epochs and their epoch-tagged state (a previous call may have used
+    // another formula with another layout)
+    err = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(epoch, 0, (size_t)S * 4, st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(asg, 0, (size_t)(S * n_pad), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(cst, 0, (size_t)(S * m_pad * 4), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(dh, 0, (size_t)(S * n_pad * 4), st);
+    if (err != cudaSuccess) return cuda_error(err, "gpsat_bcp_run_static: clearing the static scratch");
+    if (n_trails == 0) return GPSAT_OK;
+
+    bcp::Dev d;
+    d.n_vars = f->h.n_vars;
+    d.n_clauses = (int32_t)f->h.n_clauses();
+    d.lits = f->d_lits;
+    d.w0off = f->d_w0off;
+    d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
+    d.asg = asg;
+    d.cst = cst;
+    d.dh = dh;
+    d.arena = arena;
+    d.stack = stack;
+    d.epoch = epoch;
+    d.next_trail = counter;
+    d.n_pad = n_pad;
+    d.m_pad = m_pad;
+    d.arena_cap = acap;
+    d.impl_cap = impl_cap;
+    d.n_slots = (int32_t)S;
+    d.trail = trail_lits;
+    d.toff = trail_offsets;
+    d.n_trails = n_trails;
+    d.status = status;
+    d.conflict = conflict_clause;
+    d.stop = stop_index;
+    d.nimpl = n_impl;
+    d.ilit = impl_lit;
+    d.ireason = impl_reason;
+    d.counters = counters;
+    const int blocks = (int)((S + bcp::WARPS - 1) / bcp::WARPS);
+    bcp::bcp_kernel<<<blocks, bcp::WARPS * 32, 0, st>>>(d);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch (static scratch)");
     return GPSAT_OK;
 }

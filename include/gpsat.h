@@ -131,6 +131,33 @@ int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *t
 /* Trails in flight and the device bytes the workspace holds. */
 int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
 
+/* Allocation-free BCP (no counterpart in the reference, whose BCP allocates
+ * its watch-node pool and graph up front): the same kernel and outputs as
+ * gpsat_bcp_run_device, but the per-trail state lives in one fixed 64 MiB
+ * device array inside the library (GPSAT_BCP_STATIC_SCRATCH_BYTES), and the
+ * call makes no cudaMalloc, cudaFree or other allocating call.  It is for
+ * callers that cannot allocate at propagation time: code capturing the call
+ * into a CUDA graph (device allocation is not allowed on a capturing stream,
+ * and a replayed graph needs fixed addresses), and hosts whose device memory
+ * is reserved up front by their own pool.
+ *   f      must already be resident on the device: gpsat_bcp_create on it
+ *          uploads it (the upload allocates, so do it beforehand).
+ *   impl_cap, arena_cap  as in gpsat_bcp_create (arena_cap 0 = default).
+ * As many trails run at once as fit in the array (at most the resident warp
+ * count); if one trail's state does not fit, the call returns
+ * GPSAT_ERR_CAPACITY and launches nothing.  The state that must start at
+ * zero is cleared on the stream by every call.
+ * The first call on a device looks the array up (and may load the module):
+ * make that first call before any stream capture begins.
+ * One array per device: calls whose GPU work overlaps (e.g. on two streams)
+ * race on it and give wrong results; order them on one stream. */
+#define GPSAT_BCP_STATIC_SCRATCH_BYTES ((int64_t)64 << 20)
+int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, int64_t arena_cap,
+                         const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails,
+                         int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                         int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason,
+                         int64_t *counters, void *stream);
+
 /* ---- CDCL solving on the device -------------------------------------------
  * One warp runs one complete CDCL search (two watched literals, first-UIP
  * learning, VSIDS, restarts) for one job; a persistent grid pulls jobs from a
