@@ -58,6 +58,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-trails", type=int, default=1024)
+    ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted"],
+                    help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
+                         "planted: planted community instances split into JobChooser cubes")
+    ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 1024")
+    ap.add_argument("--depth", type=int, default=6, help="planted: split variables per instance (cubes = 2^depth)")
+    ap.add_argument("--cpu-instances", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=30.0)
     return ap.parse_args()
 
 
@@ -306,9 +313,222 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- batched solving
+SOLVE_METRIC = "instances decided/s"
+
+
+def solve_instances(count, first=0):
+    """Seeded random 3-SAT, n ~ U[50, 250], m = round(4.26 n): instance i uses
+    formula seed 5000 + i; the sizes come from one seeded stream."""
+    import gpupsat_gb300 as g
+    ns = np.random.default_rng(11).integers(50, 251, size=first + count)[first:]
+    return [(int(n), *g.gen_random_ksat(5000 + first + i, int(n), int(round(4.26 * n)), 3))
+            for i, n in enumerate(ns)]
+
+
+def solve_config(args):
+    return {"workload": "batched solve: random 3-SAT, n ~ U[50,250], m = round(4.26 n)",
+            "instances": args.instances, "conflict_budget": 100000, "decisions": "VSIDS", "restarts": "Luby 100",
+            "l2": "per-job state > L2 (one workspace slot per resident warp); no flush needed"}
+
+
+def _ref_solve_one(job):
+    """Worker: the reference's own solver (host build of its sources) on one instance."""
+    import ctypes
+    variant, n, lits, off = job
+    from oracle.ref import build_ref
+    L = ctypes.CDLL(str(build_ref.OUT / f"libref_{variant}_{__import__('platform').machine()}.so"))
+    vp = ctypes.c_void_p
+    L.ref_solve.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64, vp]
+    L.ref_solve.restype = ctypes.c_int
+    model = np.zeros(n, np.int32)
+    t0 = time.perf_counter()
+    v = L.ref_solve(lits.ctypes.data, off.ctypes.data, n, len(off) - 1, model.ctypes.data)
+    return v, time.perf_counter() - t0
+
+
+def ref_solve_sample(args, variant="stock"):
+    """Times the reference's solver on a bounded sample of the same instances
+    with one process per host core; instances still running at the deadline
+    count as undecided."""
+    import multiprocessing as mp
+    inst = solve_instances(args.cpu_instances)
+    procs = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    decided = done = 0
+    pool = ctx.Pool(procs)
+    t0 = time.perf_counter()
+    try:
+        it = pool.imap_unordered(_ref_solve_one, [(variant, n, l, o) for n, l, o in inst])
+        while True:
+            left = args.cpu_seconds - (time.perf_counter() - t0)
+            if left <= 0:
+                break
+            try:
+                v, _ = it.next(timeout=left)
+            except StopIteration:
+                break
+            except mp.TimeoutError:
+                break
+            done += 1
+            decided += v in (10, 20)
+    finally:
+        dt = time.perf_counter() - t0
+        pool.terminate()
+    return decided / dt, decided, done, len(inst), dt, procs
+
+
+def run_solve_reference(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    v, decided, done, total, dt, procs = ref_solve_sample(args, "stock")
+    line = {"impl": "reference", "metric": SOLVE_METRIC, "value": v, "unit": "instances/s", "n_gpus": args.gpus,
+            "steps": 1, "warmup": 0, "ms_per_step": 1000 * dt, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded uniform random 3-SAT",
+            "config": solve_config(args),
+            "cpu_baseline": {"value": v, "unit": "instances/s", "cores": procs, "kind": "reference",
+                             "sample": f"first {total} instances, {args.cpu_seconds:.0f} s wall budget: {decided} "
+                                       f"decided, {done} returned (stock MAX_ITERATIONS=1000 returns UNDEF)"},
+            "e2e": {"value": v, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def planted_instances(count, first=0):
+    """Planted 3-SAT, n ~ U[2000, 20000], m = 4.0 n, 40 equal communities, 90% of
+    a clause's variables from its community; instance i uses seed 9000 + i."""
+    import gpupsat_gb300 as g
+    ns = np.random.default_rng(13).integers(2000, 20001, size=first + count)[first:]
+    out = []
+    for i, n in enumerate(ns):
+        lits, off, _ = g.gen_planted(9000 + first + i, int(n), 4 * int(n), 3, 40, 0.9)
+        out.append((int(n), lits, off))
+    return out
+
+
+def run_planted_gpu(args):
+    import torch
+    import gpupsat_gb300 as g
+    from gpupsat_gb300 import jobs
+    torch.cuda.set_device(0)
+    inst = planted_instances(args.instances)
+    formulas = [(l, o) for _, l, o in inst]
+    nv = [n for n, _, _ in inst]
+    jf, co, cl = jobs.cube_jobs(formulas, nv, args.depth)
+    opts = g.solve_options()
+    b = g.Batch(formulas, nv)
+    for _ in range(args.warmup):
+        out = b.solve(opts, jobs=(jf, co, cl))
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = b.solve(opts, jobs=(jf, co, cl))
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    v = out["verdict"]
+    st = out["stats"]
+    decided = int((v != 0).sum())
+    assert (out["model_ok"][v == 10] == 1).all(), "a SAT verdict without a verified model"
+    e2e_t = []
+    for _ in range(max(1, min(2, args.steps))):
+        t0 = time.perf_counter()
+        bb = g.Batch(formulas, nv)
+        bb.solve(opts, jobs=(jf, co, cl))
+        e2e_t.append(time.perf_counter() - t0)
+        bb.close()
+    h2d = sum(l.nbytes + o.nbytes for l, o in formulas) + jf.nbytes + co.nbytes + cl.nbytes
+    d2h = int(out["verdict"].nbytes + out["model"].nbytes + out["stats"].nbytes + out["model_ok"].nbytes)
+    line = {"metric": "instances decided/s", "value": decided * args.steps / sum(times), "unit": "instances/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded planted 3-SAT with 40 communities",
+            "config": {"workload": "structured batch: planted community 3-SAT, n ~ U[2000,20000], m = 4.0 n",
+                       "instances": args.instances, "cube_depth": args.depth, "jobs": int(len(jf)),
+                       "chooser": "MaxClauseJobChooser ranking (reference VariableChooser score)",
+                       "l2": "per-job state > L2; no flush needed"},
+            "cpu_baseline": None, "clocks": clk,
+            "e2e": {"value": decided * len(e2e_t) / sum(e2e_t), "unit": "instances/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": 2 * args.steps,
+            "verdicts": {"sat": int((v == 10).sum()), "unsat": int((v == 20).sum()), "unknown": int((v == 0).sum())},
+            "conflicts_per_instance": {"median": float(np.median(st[:, 0])), "max": int(st[:, 0].max())},
+            "props_per_s": float(st[:, 2].sum()) * args.steps / sum(times)}
+    print(json.dumps(line))
+
+
+def run_solve_gpu(args):
+    import torch
+    import gpupsat_gb300 as g
+    torch.cuda.set_device(0)
+    inst = solve_instances(args.instances)
+    formulas = [(l, o) for _, l, o in inst]
+    nv = [n for n, _, _ in inst]
+    opts = g.solve_options()
+    b = g.Batch(formulas, nv)
+    for _ in range(args.warmup):
+        out = b.solve(opts)
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = b.solve(opts)
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    v = out["verdict"]
+    decided = int((v != 0).sum())
+    st = out["stats"]
+    value = decided * args.steps / sum(times)
+    # end to end: upload + solve + results back, from the host CNF arrays
+    e2e_t = []
+    for _ in range(max(1, min(2, args.steps))):
+        t0 = time.perf_counter()
+        bb = g.Batch(formulas, nv)
+        bb.solve(opts)
+        e2e_t.append(time.perf_counter() - t0)
+        bb.close()
+    h2d = sum(l.nbytes + o.nbytes for l, o in formulas)
+    d2h = int(out["verdict"].nbytes + out["model"].nbytes + out["stats"].nbytes + out["model_ok"].nbytes)
+    cpu = None
+    if not args.no_cpu:
+        rv, rdec, rdone, rtot, rdt, procs = ref_solve_sample(args, "stock")
+        cpu = {"value": rv, "unit": "instances/s", "cores": procs, "kind": "reference",
+               "sample": f"first {rtot} instances, {args.cpu_seconds:.0f} s wall budget: {rdec} decided"}
+    line = {"metric": SOLVE_METRIC, "value": value, "unit": "instances/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded uniform random 3-SAT",
+            "config": solve_config(args), "cpu_baseline": cpu, "clocks": clk,
+            "e2e": {"value": decided * len(e2e_t) / sum(e2e_t), "unit": "instances/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": 2 * args.steps,
+            "verdicts": {"sat": int((v == 10).sum()), "unsat": int((v == 20).sum()), "unknown": int((v == 0).sum())},
+            "conflicts": {"median": float(np.median(st[:, 0])), "mean": float(st[:, 0].mean()),
+                          "max": int(st[:, 0].max())},
+            "conflicts_per_s": float(st[:, 0].sum()) * args.steps / sum(times),
+            "props_per_s": float(st[:, 2].sum()) * args.steps / sum(times)}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.instances is None:
+        args.instances = 1024 if args.workload == "planted" else 16384
+    if args.workload == "planted":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's host-built solver did not return "
+                              "within 600 s on one n=2000 planted instance (seed 9000) on an x86 host core; "
+                              "see --workload solve for its timed baseline"}))
+        else:
+            run_planted_gpu(args)
+    elif args.workload == "solve":
+        if args.impl == "reference":
+            run_solve_reference(args)
+        else:
+            run_solve_gpu(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

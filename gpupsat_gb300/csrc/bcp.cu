@@ -42,8 +42,10 @@
 // that could have changed a later evaluation: an entry whose clause an earlier
 // entry of the round already handled, a later scan whose list is not what the
 // round assumed (it has clauses add_first'ed to it, possibly by this round),
-// or the entry just after an implication or a conflict.  Events are encoded as
-// ordered keys and the cut is one warp min-reduction.  Uncommitted entries are
+// the entry just after a conflict, the end of the scan an implication was
+// found in (its depth-first descent comes first), or a later entry of that
+// scan whose clause has the implied variable.  Events are encoded as ordered
+// keys and the cut is one warp min-reduction.  Uncommitted entries are
 // evaluated again next round, so the result is the sequential one.
 #include <cuda_runtime.h>
 
@@ -574,7 +576,26 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             const int keyc = has ? en.x : -1 - lane;
             const unsigned mm = __match_any_sync(FULL, keyc);
             if (has && (mm & lt)) key = key_before(lane, my_scan);  // clause seen earlier this round
-            if (valid && (r.act == A_IMPLY || r.act == A_CONFLICT)) key = min(key, key_after(lane, my_scan));
+            if (valid && r.act == A_CONFLICT) key = min(key, key_after(lane, my_scan));
+            // an implication ends its scan's part of the window (its depth-first
+            // descent comes before any later scan) ...
+            const bool imp = valid && r.act == A_IMPLY;
+            if (imp) key = min(key, key_after(sm.sc_end[my_scan] - 1, my_scan));
+            // ... and a later entry of the same scan is evaluated again if its
+            // clause has the implied variable (a long clause: always); the
+            // other entries read nothing the implication changed
+            unsigned im = __ballot_sync(FULL, imp);
+            while (im) {
+                const int k = __ffs(im) - 1;
+                im &= im - 1;
+                const int32_t uv = __shfl_sync(FULL, r.unit >> 1, k);
+                const int ks = __shfl_sync(FULL, my_scan, k);
+                if (valid && lane > k && my_scan == ks) {
+                    const bool dep = en.z > KIN || (el.x >> 1) == uv || (en.z > 1 && (el.y >> 1) == uv) ||
+                                     (en.z > 2 && (el.z >> 1) == uv) || (en.z > 3 && (el.w >> 1) == uv);
+                    if (dep) key = min(key, key_before(lane, my_scan));
+                }
+            }
             // a later window scan whose list starts with added clauses
             if (scan_v >= 0 && (scan_h >> 24) == e) key = min(key, key_before(scan_b, lane));
             // a move of this lane that lands in a later window scan's list
@@ -601,6 +622,19 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             new_started = (cut & 1) || new_cur == 0 || k_end > sm.sc_begin[new_cur];
         }
 
+        // more implications than impl_cap leaves room for: commit up to the
+        // first one that does not fit; the next round reports the overflow there
+        {
+            const unsigned im0 = __ballot_sync(FULL, valid && lane < k_end && r.act == A_IMPLY);
+            const int64_t room = d.impl_cap - n_impl;
+            if (room > 0 && __popc(im0) > room) {
+                const int kk = nth_set_bit(im0, (int)room + 1);
+                const int ks = __shfl_sync(FULL, my_scan, kk);
+                k_end = kk;
+                new_cur = ks;
+                new_started = ks == 0 || kk > sm.sc_begin[ks];
+            }
+        }
         const bool com = valid && lane < k_end;
         // watch moves: add_first into the target var's list, in commit order
         const bool ins1 = com && (r.act == A_SW1 || r.act == A_SW2);
@@ -677,16 +711,16 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             else ns = (e << 24) | (1u << 22) | ((uint32_t)w1 << 11) | (uint32_t)w2;
             cst[en.x] = ns;
         }
-        // implication (at most one per round: it ends the commit)
+        // implications, in commit order (all of one scan, on distinct variables)
         if (imask) {
-            const int k = __ffs(imask) - 1;
-            if (lane == k) {
-                ilit[n_impl] = dimacs_of(r.unit);
-                ireason[n_impl] = en.x;
+            if ((imask >> lane) & 1u) {
+                const int64_t at = n_impl + __popc(imask & lt);
+                ilit[at] = dimacs_of(r.unit);
+                ireason[at] = en.x;
                 asg[r.unit >> 1] = (uint8_t)((e << 1) | (uint32_t)(r.unit & 1));
             }
-            n_impl++;
-            cI++;
+            n_impl += __popc(imask);
+            cI += __popc(imask);
         }
         const unsigned cmask = __ballot_sync(FULL, com && r.act == A_CONFLICT);
         if (com) {
@@ -725,7 +759,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             dfs_trail = cur_trail;
             ti += new_cur;
             cur_is_trail = true;
-            cur_impl_start = n_impl - (imask ? 1 : 0);
+            cur_impl_start = n_impl - __popc(imask);
         }
         if (cmask) {
             const int k = __ffs(cmask) - 1;
@@ -757,9 +791,11 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     }
 }
 
-// blocks per SM the register allocation targets (8 = 32 resident warps per SM)
+// blocks per SM the register allocation targets: 4 (16 resident warps per SM)
+// leaves the kernel its ~100 registers without spills, which measured faster
+// than 32 resident warps with spills at 64 registers
 #ifndef GPSAT_BCP_MIN_BLOCKS
-#define GPSAT_BCP_MIN_BLOCKS 8
+#define GPSAT_BCP_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(WARPS * 32, GPSAT_BCP_MIN_BLOCKS) bcp_kernel(Dev d)
 {

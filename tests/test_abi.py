@@ -100,3 +100,18 @@ def test_bcp_without_device_fails_loudly(gpsat):
     with pytest.raises(gpsat.GpsatError) as e:
         gpsat.BCPBatch(f, impl_cap=64)
     assert e.value.code == -7
+
+
+def test_cube_jobs_follow_the_reference_chooser(gpsat):
+    from gpupsat_gb300 import jobs
+    # var 3 occurs 3 times (score 3*2), var 2 twice (2*1), var 1 once (0)
+    lits = np.array([1, 2, 3, -2, 3, -3], np.int32)
+    assert list(jobs.rank_variables(lits, 3)) == [3, 2, 1]
+    assert list(jobs.rank_variables(lits, 3, "occurrences")) == [3, 2, 1]
+    assert list(jobs.rank_variables(lits, 3, scores=[5.0, 1.0, 5.0])) == [1, 3, 2]
+    jf, co, cl = jobs.cube_jobs([(lits, np.array([0, 3, 6]))], [3], depth=2)
+    assert list(jf) == [0] * 4 and list(co) == [0, 2, 4, 6, 8]
+    # depth first, positive before negative
+    assert cl.reshape(4, 2).tolist() == [[3, 2], [3, -2], [-3, 2], [-3, -2]]
+    jf, co, cl = jobs.cube_jobs([(lits, None), (lits, None)], [3, 3], depth=0)
+    assert list(jf) == [0, 1] and list(co) == [0, 0, 0] and len(cl) == 0
