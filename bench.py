@@ -58,10 +58,15 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-trails", type=int, default=1024)
-    ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted"],
+    ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding"],
                     help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
-                         "planted: planted community instances split into JobChooser cubes")
-    ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 1024")
+                         "planted: planted community instances split into JobChooser cubes; "
+                         "seeding: learned VSIDS/phase seeding against plain solving")
+    ap.add_argument("--n-range", type=int, nargs=2, default=[50, 250], help="solve: variables per instance")
+    ap.add_argument("--conflict-budget", type=int, default=100000, help="solve/planted/seeding: per job")
+    ap.add_argument("--train-instances", type=int, default=4096, help="seeding: training formulas")
+    ap.add_argument("--epochs", type=int, default=3, help="seeding: training passes")
+    ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 1024, seeding: 1024 held-out formulas")
     ap.add_argument("--depth", type=int, default=6, help="planted: split variables per instance (cubes = 2^depth)")
     ap.add_argument("--cpu-instances", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
@@ -138,14 +143,15 @@ def peaks():
 
 
 def traffic_per_launch(n, trails):
-    """DRAM bytes per launch from the committed ncu summary, scaled by trail count."""
+    """DRAM bytes of one launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed capture of this exact workload, else None."""
     p = ROOT / "profiles" / "bcp_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    if d.get("n_vars") != n:
+    if d.get("n_vars") != n or d.get("n_trails") != trails:
         return None
-    return d["dram_bytes_per_trail"] * trails
+    return d["dram_bytes_per_launch"]
 
 
 def alg_bytes(cnt):
@@ -317,18 +323,20 @@ def run_gpu(args):
 SOLVE_METRIC = "instances decided/s"
 
 
-def solve_instances(count, first=0):
-    """Seeded random 3-SAT, n ~ U[50, 250], m = round(4.26 n): instance i uses
+def solve_instances(count, first=0, n_range=(50, 250)):
+    """Seeded random 3-SAT, n ~ U[n_range], m = round(4.26 n): instance i uses
     formula seed 5000 + i; the sizes come from one seeded stream."""
     import gpupsat_gb300 as g
-    ns = np.random.default_rng(11).integers(50, 251, size=first + count)[first:]
+    ns = np.random.default_rng(11).integers(n_range[0], n_range[1] + 1, size=first + count)[first:]
     return [(int(n), *g.gen_random_ksat(5000 + first + i, int(n), int(round(4.26 * n)), 3))
             for i, n in enumerate(ns)]
 
 
 def solve_config(args):
-    return {"workload": "batched solve: random 3-SAT, n ~ U[50,250], m = round(4.26 n)",
-            "instances": args.instances, "conflict_budget": 100000, "decisions": "VSIDS", "restarts": "Luby 100",
+    lo, hi = args.n_range
+    return {"workload": f"batched solve: random 3-SAT, n ~ U[{lo},{hi}], m = round(4.26 n)",
+            "instances": args.instances, "conflict_budget": args.conflict_budget, "decisions": "VSIDS",
+            "restarts": "Luby 100",
             "l2": "per-job state > L2 (one workspace slot per resident warp); no flush needed"}
 
 
@@ -352,7 +360,7 @@ def ref_solve_sample(args, variant="stock"):
     with one process per host core; instances still running at the deadline
     count as undecided."""
     import multiprocessing as mp
-    inst = solve_instances(args.cpu_instances)
+    inst = solve_instances(args.cpu_instances, n_range=args.n_range)
     procs = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     decided = done = 0
@@ -414,7 +422,7 @@ def run_planted_gpu(args):
     formulas = [(l, o) for _, l, o in inst]
     nv = [n for n, _, _ in inst]
     jf, co, cl = jobs.cube_jobs(formulas, nv, args.depth)
-    opts = g.solve_options()
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
     b = g.Batch(formulas, nv)
     for _ in range(args.warmup):
         out = b.solve(opts, jobs=(jf, co, cl))
@@ -458,14 +466,88 @@ def run_planted_gpu(args):
     print(json.dumps(line))
 
 
+def run_seeding_gpu(args):
+    """Learned seeding: train the network on budgeted solves of a random k-SAT
+    training set, then solve held-out 3-SAT (n = 300, ratio 4.26) plain and
+    seeded.  value = seeded instances decided/s including the network's
+    inference; the plain arm and the network's own throughput ride along."""
+    import torch
+    import gpupsat_gb300 as g
+    from gpupsat_gb300 import learn
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda:0")
+    t0 = time.perf_counter()
+    data = learn.training_set(args.train_instances, seed=0)
+    net = learn.SeedNet(dev, seed=0)
+    hist, _ = learn.train(net, data, epochs=args.epochs, log=lambda m: print(m, file=sys.stderr))
+    train_s = time.perf_counter() - t0
+    held = [(300, *g.gen_random_ksat(40000 + i, 300, 1278, 3)) for i in range(args.instances)]
+    formulas = [(l, o) for _, l, o in held]
+    nv = [n for n, _, _ in held]
+    b = g.Batch(formulas, nv)
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
+    out_plain = b.solve(opts)                      # warm-up (and the plain arm's verdicts)
+    t0 = time.perf_counter()
+    out_plain = b.solve(opts)
+    plain_s = time.perf_counter() - t0
+    # seeded: inference + seeds + solve, end to end from the host CNF arrays
+    score, phase = learn.predict(net, formulas, nv)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    score, phase = learn.predict(net, formulas, nv)
+    infer_s = time.perf_counter() - t0
+    act, ph = learn.seeds_from(score, phase)
+    b.set_seeds(act, ph)
+    t0 = time.perf_counter()
+    out_seed = b.solve(opts)
+    seed_solve_s = time.perf_counter() - t0
+    # the network's forward throughput on the held-out graph (device time)
+    G = learn.Graph(formulas, nv, dev)
+    ps = learn.Pass(net, G)
+    ps.forward()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    ev0.record()
+    for _ in range(reps):
+        ps.forward()
+    ev1.record()
+    torch.cuda.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / reps
+    D = learn.D
+    flops = learn.LAYERS * (2 * G.V * D * 3 * D + 2 * G.C * D * D + 2 * G.C * D * 2 * D)
+    vp, vs = out_plain["verdict"], out_seed["verdict"]
+    assert (vp[(vp != 0) & (vs != 0)] == vs[(vp != 0) & (vs != 0)]).all(), "seeded and plain verdicts disagree"
+    assert (out_seed["model_ok"][vs == 10] == 1).all()
+    dec_p, dec_s = int((vp != 0).sum()), int((vs != 0).sum())
+    value = dec_s / (infer_s + seed_solve_s)
+    line = {"metric": "instances decided/s (learned seeding)", "value": value, "unit": "instances/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": 1000 * (infer_s + seed_solve_s), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, int32 solver",
+            "data": "synthetic: seeded random k-SAT (training) and 3-SAT n=300 ratio 4.26 (held out)",
+            "config": {"workload": "learned seeding: 3-layer 64-wide message passing, VSIDS + phase seeds",
+                       "train_instances": args.train_instances, "epochs": args.epochs, "held_out": args.instances,
+                       "conflict_budget": args.conflict_budget, "train_seconds": round(train_s, 1),
+                       "final_losses": [round(float(x), 4) for x in hist[-1]]},
+            "plain": {"decided_per_s": dec_p / plain_s, "decided": dec_p,
+                      "median_conflicts": float(np.median(out_plain["stats"][:, 0]))},
+            "seeded": {"decided_per_s": value, "decided": dec_s,
+                       "median_conflicts": float(np.median(out_seed["stats"][:, 0])),
+                       "inference_ms": 1000 * infer_s},
+            "network": {"forward_ms": fwd_ms, "tflops": flops / (fwd_ms * 1e-3) / 1e12, "nodes": G.V + G.C,
+                        "edges": G.E},
+            "gpu_launches": None}
+    print(json.dumps(line))
+
+
 def run_solve_gpu(args):
     import torch
     import gpupsat_gb300 as g
     torch.cuda.set_device(0)
-    inst = solve_instances(args.instances)
+    inst = solve_instances(args.instances, n_range=args.n_range)
     formulas = [(l, o) for _, l, o in inst]
     nv = [n for n, _, _ in inst]
-    opts = g.solve_options()
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
     b = g.Batch(formulas, nv)
     for _ in range(args.warmup):
         out = b.solve(opts)
@@ -515,8 +597,14 @@ def run_solve_gpu(args):
 def main():
     args = parse()
     if args.instances is None:
-        args.instances = 1024 if args.workload == "planted" else 16384
-    if args.workload == "planted":
+        args.instances = {"planted": 1024, "seeding": 1024}.get(args.workload, 16384)
+    if args.workload == "seeding":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned seeding; its "
+                              "solver's timed baseline is --workload solve"}))
+        else:
+            run_seeding_gpu(args)
+    elif args.workload == "planted":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference's host-built solver did not return "
                               "within 600 s on one n=2000 planted instance (seed 9000) on an x86 host core; "

@@ -92,6 +92,24 @@ def _declare(L: ctypes.CDLL) -> None:
                                             ctypes.c_double, _vp, _vp]),
         "gpsat_gen_planted": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_double, _vp, _vp]),
+        # learned seeding kernels (device pointers)
+        "gpsat_gnn_mm": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32,
+                                        ctypes.c_int32, _vp, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp]),
+        "gpsat_gnn_wgrad": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                           _vp, _vp]),
+        "gpsat_gnn_gather": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int32, _vp, _vp,
+                                            ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp]),
+        "gpsat_gnn_gather_split": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int32, _vp, _vp, _vp,
+                                                  ctypes.c_int32, _vp]),
+        "gpsat_gnn_relu_bwd": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int64, _vp,
+                                              ctypes.c_int32, _vp]),
+        "gpsat_gnn_colsum": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int64, _vp, _vp]),
+        "gpsat_gnn_broadcast": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, ctypes.c_int32, _vp]),
+        "gpsat_gnn_head": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int64] + [_vp] * 8 + [ctypes.c_int32, _vp, _vp,
+                                                                                               _vp]),
+        "gpsat_gnn_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_float, ctypes.c_int64, _vp]),
+        "gpsat_gnn_pack": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

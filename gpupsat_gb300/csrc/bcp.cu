@@ -306,18 +306,33 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 }
             } else {
                 if (ti >= tn) break;
-                int32_t x = d.trail[tb + ti];
-                v = (x > 0 ? x : -x) - 1;
+                v = -1;
+                const int64_t bo = ti - lb_base;
+                if (bo >= 0 && bo < 32) {
+                    // the look-ahead buffer holds this position's variable and range
+                    v = __shfl_sync(FULL, lb_v, (int)bo);
+                    cur_wk = __shfl_sync(FULL, lb_a, (int)bo);
+                    cur_wend = __shfl_sync(FULL, lb_b, (int)bo);
+                } else {
+                    int32_t x = d.trail[tb + ti];
+                    v = (x > 0 ? x : -x) - 1;
+                }
                 cur_trail = ti;
                 dfs_trail = ti;
                 ti++;
                 cur_is_trail = true;
+                if (bo < 0 || bo >= 32) {
+                    cur_wk = d.w0off[v];
+                    cur_wend = d.w0off[v + 1];
+                }
             }
             uint32_t h = dh[v];
             cur_var = v;
             cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-            cur_wk = d.w0off[v];
-            cur_wend = d.w0off[v + 1];
+            if (!cur_is_trail) {
+                cur_wk = d.w0off[v];
+                cur_wend = d.w0off[v + 1];
+            }
             cur_counted = false;
             cur_impl_start = n_impl;
             in_scan = true;
@@ -327,15 +342,22 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             cur_counted = true;
         }
         if (cur_dp < 0 && cur_wk >= cur_wend) {
-            // scan finished: descend into the implications it found
-            in_scan = false;
-            if (n_impl > cur_impl_start) {
-                if (depth > 0 && lane == 0) stk[depth - 1] = make_int2((int)top_j, (int)top_e);
-                top_j = cur_impl_start;
-                top_e = n_impl;
-                depth++;
+            // scan finished.  A trail scan that implied nothing leads straight
+            // to the next trail scans: this round's window is those alone (as
+            // look-ahead scans, set up from the look-ahead buffer with their
+            // list heads loaded in the round's own trip), not a separate setup
+            const bool next_trail_scans = depth == 0 && cur_is_trail && n_impl == cur_impl_start && ti < tn;
+            if (!next_trail_scans) {
+                // descend into the implications it found
+                in_scan = false;
+                if (n_impl > cur_impl_start) {
+                    if (depth > 0 && lane == 0) stk[depth - 1] = make_int2((int)top_j, (int)top_e);
+                    top_j = cur_impl_start;
+                    top_e = n_impl;
+                    depth++;
+                }
+                continue;
             }
-            continue;
         }
 
         // ---- gather the window
@@ -386,6 +408,11 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                     lb_v = (x > 0 ? x : -x) - 1;
                     lb_a = d.w0off[lb_v];
                     lb_b = d.w0off[lb_v + 1];
+                    // warm L2 with these scans' initial watch entries (up to 32
+                    // each, four 32-byte entries per line): the rounds of the
+                    // next 16-32 trail scans gather them
+                    for (uint32_t w = lb_a; w < lb_b && w < lb_a + 32; w += 4)
+                        asm volatile("prefetch.L2 [%0];" ::"l"(d.w0ent + 2 * (size_t)w));
                 }
             }
             const int lb_off = (int)(ti - lb_base);

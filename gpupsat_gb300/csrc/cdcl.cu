@@ -85,6 +85,8 @@ struct Ctx {
     uint8_t *seen;
     int32_t *level, *reason, *trail, *tlim, *learnt, *lstamp, *tmp;
     float *act;
+    float *bmax;     // per block of 32 variables: >= the largest activity of its unassigned
+                     // variables (-1: none left); exact for a block pick_branch last tightened
     int32_t *wl_start, *wl_size, *wl_cap, *wl_cnt;
     int2 *watches;
     int32_t *arena, *crefs;
@@ -414,16 +416,26 @@ __device__ int32_t propagate(Ctx &C)
 }
 
 // ---------------------------------------------------------------- analysis
+// Activities are >= 0, so their float bits order like ints: atomicMax on the
+// bits raises a block bound.
+__device__ __forceinline__ void raise_bound(Ctx &C, int32_t v, float a)
+{
+    atomicMax(reinterpret_cast<int *>(&C.bmax[v >> 5]), __float_as_int(a));
+}
+
 __device__ __forceinline__ void bump(Ctx &C, int32_t v, bool &big)
 {
     float a = C.act[v] + C.var_inc;
     C.act[v] = a;
+    raise_bound(C, v, a);
     big |= a > 1e30f;
 }
 
 __device__ void rescale(Ctx &C)
 {
     for (int v = C.lane; v < C.n; v += 32) C.act[v] *= 1e-30f;
+    for (int b = C.lane; b < (C.n + 31) / 32; b += 32)
+        if (C.bmax[b] >= 0.f) C.bmax[b] *= 1e-30f;
     C.var_inc *= 1e-30f;
     __syncwarp();
 }
@@ -580,6 +592,7 @@ __device__ void backtrack(Ctx &C, int lvl)
         const int32_t l = C.trail[k];
         C.phase[l >> 1] = (int8_t)(l & 1);
         C.val[l >> 1] = 0;
+        raise_bound(C, l >> 1, C.act[l >> 1]);
     }
     C.tsize = from;
     C.qhead = from;
@@ -728,28 +741,51 @@ __device__ int32_t pick_branch(Ctx &C, int mode)
         best = wmax(best);
         return best < 0 ? -1 : 2 * best + 1;
     }
-    float ba = -FLT_MAX;
-    int bv = -1;
-    for (int v = lane; v < C.n; v += 32) {
-        if (C.val[v] == 0) {
-            const float a = C.act[v];
-            if (bv < 0 || a > ba) {
-                ba = a;
-                bv = v;
+    // VSIDS: the unassigned variable of largest activity, lowest index on ties.
+    // Take the block with the largest bound (lowest block on ties), compute its
+    // exact best; if that reaches the bound it beats every other block, else
+    // tighten the bound and look again.  Every round either answers or makes one
+    // bound exact, so the loop ends; the answer is the full scan's.
+    const int nb = (C.n + 31) / 32;
+    for (int guard = 0; guard <= 2 * nb + 1; guard++) {
+        float bb = -2.f;
+        int bi = -1;
+        for (int b = lane; b < nb; b += 32) {
+            const float x = C.bmax[b];
+            if (x > bb) {
+                bb = x;
+                bi = b;
             }
         }
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float oa = __shfl_xor_sync(FULL, ba, o);
-        const int ov = __shfl_xor_sync(FULL, bv, o);
-        if (ov >= 0 && (bv < 0 || oa > ba || (oa == ba && ov < bv))) {
-            ba = oa;
-            bv = ov;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(FULL, bb, o);
+            const int oi = __shfl_xor_sync(FULL, bi, o);
+            if (oi >= 0 && (bi < 0 || ob > bb || (ob == bb && oi < bi))) {
+                bb = ob;
+                bi = oi;
+            }
         }
+        if (bi < 0 || bb < 0.f) return -1;  // no unassigned variable left
+        const int v = 32 * bi + lane;
+        const bool free_v = v < C.n && C.val[v] == 0;
+        float ba = free_v ? C.act[v] : -1.f;
+        int bv = free_v ? v : -1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(FULL, ba, o);
+            const int ov = __shfl_xor_sync(FULL, bv, o);
+            if (ov >= 0 && (bv < 0 || oa > ba || (oa == ba && ov < bv))) {
+                ba = oa;
+                bv = ov;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) C.bmax[bi] = bv < 0 ? -1.f : ba;
+        __syncwarp();
+        if (bv >= 0 && ba >= bb) return 2 * bv + (C.phase[bv] ? 1 : 0);
     }
-    if (bv < 0) return -1;
-    return 2 * bv + (C.phase[bv] ? 1 : 0);
+    return -1;  // not reached: every round tightens a bound
 }
 
 __device__ __forceinline__ double luby(double y, int x)
@@ -804,6 +840,12 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
         C.phase[v] = P.seed_phase ? P.seed_phase[voff + v] : (int8_t)o.phase_init;
     }
     for (int v = lane; v <= C.n; v += 32) C.lstamp[v] = 0;
+    __syncwarp();
+    for (int b = lane; b < (C.n + 31) / 32; b += 32) {
+        float x = 0.f;
+        for (int v = 32 * b; v < 32 * b + 32 && v < C.n; v++) x = fmaxf(x, C.act[v]);
+        C.bmax[b] = x;
+    }
     // copy the clauses into the arena
     const uint32_t base = P.coff[cb];
     const int64_t otop = (int64_t)(P.coff[ce] - base) + (int64_t)HDR * m;
@@ -970,26 +1012,54 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
 __global__ void __launch_bounds__(WARPS * 32) cdcl_kernel(Params P)
 {
     __shared__ int32_t smem[WARPS][64];
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int slot = blockIdx.x * WARPS + wib;
     if (slot >= P.n_slots) return;
     Ctx C;
     C.lane = lane;
     const size_t N = (size_t)P.N, S = (size_t)slot;
-    C.val = P.val + S * N;
-    C.phase = P.phase + S * N;
-    C.seen = P.seen + S * N;
-    C.level = P.level + S * N;
-    C.reason = P.reason + S * N;
-    C.trail = P.trail + S * N;
-    C.tlim = P.tlim + S * (N + 1);
-    C.learnt = P.learnt + S * (N + 1);
-    C.lstamp = P.lstamp + S * (N + 1);
-    C.act = P.act + S * N;
-    C.wl_start = P.wl_start + S * 2 * N;
-    C.wl_size = P.wl_size + S * 2 * N;
-    C.wl_cap = P.wl_cap + S * 2 * N;
-    C.wl_cnt = P.wl_cnt + S * 2 * N;
+    if (P.smem_per_warp > 0) {
+        // small formulas: the arrays every propagation, analysis and decision
+        // touch at random sit in this warp's part of shared memory
+        unsigned char *b = dyn_smem + (size_t)wib * (size_t)P.smem_per_warp;
+        auto carve = [&](size_t bytes) {
+            unsigned char *q = b;
+            b += bytes;
+            return q;
+        };
+        C.level = (int32_t *)carve(4 * N);
+        C.reason = (int32_t *)carve(4 * N);
+        C.trail = (int32_t *)carve(4 * N);
+        C.act = (float *)carve(4 * N);
+        C.bmax = (float *)carve(4 * (N / 16));
+        C.tlim = (int32_t *)carve(4 * (N + 16));
+        C.learnt = (int32_t *)carve(4 * (N + 16));
+        C.lstamp = (int32_t *)carve(4 * (N + 16));
+        C.wl_start = (int32_t *)carve(8 * N);
+        C.wl_size = (int32_t *)carve(8 * N);
+        C.wl_cap = (int32_t *)carve(8 * N);
+        C.wl_cnt = (int32_t *)carve(8 * N);
+        C.val = (int8_t *)carve(N);
+        C.phase = (int8_t *)carve(N);
+        C.seen = (uint8_t *)carve(N);
+    } else {
+        C.val = P.val + S * N;
+        C.phase = P.phase + S * N;
+        C.seen = P.seen + S * N;
+        C.level = P.level + S * N;
+        C.reason = P.reason + S * N;
+        C.trail = P.trail + S * N;
+        C.tlim = P.tlim + S * (N + 1);
+        C.learnt = P.learnt + S * (N + 1);
+        C.lstamp = P.lstamp + S * (N + 1);
+        C.act = P.act + S * N;
+        C.bmax = P.bmax + S * (N / 16);
+        C.wl_start = P.wl_start + S * 2 * N;
+        C.wl_size = P.wl_size + S * 2 * N;
+        C.wl_cap = P.wl_cap + S * 2 * N;
+        C.wl_cnt = P.wl_cnt + S * 2 * N;
+    }
     C.watches = P.watches + S * (size_t)P.WCAP;
     C.arena = P.arena + S * (size_t)P.ACAP;
     C.crefs = P.crefs + S * (size_t)P.CCAP;

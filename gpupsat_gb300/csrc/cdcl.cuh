@@ -38,6 +38,16 @@ struct Opts {
     int32_t check_every = 256;       // conflicts between cancellation checks
 };
 
+// Bytes of shared memory one warp needs to hold its job's per-variable and
+// per-literal arrays for N variables (N a multiple of 16): level, reason,
+// trail, activity (4N each); tlim, learnt, lstamp (4(N+16) each); the four
+// watch-list header arrays (8N each); the activity bound per block of 32
+// variables (4 N/16); value, phase, seen (N each); rounded up to 16 bytes.
+constexpr int64_t smem_bytes_per_warp(int64_t N)
+{
+    return (16 * N + 12 * (N + 16) + 32 * N + 4 * (N / 16) + 3 * N + 15) / 16 * 16;
+}
+
 struct Params {
     Opts o;
     // instances: clauses of instance i are global clause ids [inst_cb[i], inst_ce[i])
@@ -59,12 +69,15 @@ struct Params {
     int32_t *part;               // per (instance, var): conflict participation (optional)
     // workspace
     int32_t n_slots;
-    int32_t N;                   // max vars (padded)
+    int32_t N;                   // max vars (padded to 16)
+    int32_t smem_per_warp;       // > 0: the per-variable and per-literal arrays live in
+                                 // dynamic shared memory (that many bytes per warp)
     int64_t WCAP, ACAP, CCAP;
     int8_t *val, *phase;
     uint8_t *seen;
     int32_t *level, *reason, *trail, *tlim, *learnt, *lstamp, *tmp;
     float *act;
+    float *bmax;                 // per slot N/16 floats: activity bound per block of 32 variables
     int32_t *wl_start, *wl_size, *wl_cap, *wl_cnt;
     int2 *watches;
     int32_t *arena, *crefs;

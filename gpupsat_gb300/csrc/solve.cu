@@ -137,17 +137,36 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     const int64_t C = b->max_m + 3 * lfirst + 4 * (int64_t)o->learnt_inc + N + 64;
     const int64_t A = b->max_words + (C - b->max_m) * 48;
     const int64_t W = 3 * C + 8 * (int64_t)N + 256;
-    int sms = 0, per_sm = 0;
+    int sms = 0, per_sm = 0, smem_max = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel, 128, 0);
+    // the per-variable arrays go to shared memory when that costs no
+    // resident warps (the kernel's registers already cap the blocks per SM)
+    int32_t smem_warp = (int32_t)cdcl::smem_bytes_per_warp(N);
+    if (4 * (int64_t)smem_warp + 1024 > smem_max) smem_warp = 0;
+    if (smem_warp > 0) {
+        int per_sm_smem = 0;
+        if (cudaFuncSetAttribute(cdcl::cdcl_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * smem_warp) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_smem, cdcl::cdcl_kernel, 128, 4 * smem_warp) !=
+                cudaSuccess ||
+            per_sm_smem < per_sm) {
+            cudaGetLastError();
+            smem_warp = 0;
+        }
+    }
     int32_t slots = o->max_slots > 0 ? o->max_slots : std::max(1, sms * std::max(per_sm, 1) * 4);
-    const int64_t per_slot = (int64_t)N * (1 + 1 + 1 + 4 * 4) + 3 * (int64_t)(N + 1) * 4 + 4 * 2 * (int64_t)N * 4 +
-                             W * 8 + A * 4 + C * 8;
+    // per-variable arrays in HBM only when they are not in shared memory
+    const int64_t NV = smem_warp > 0 ? 0 : N;
+    const int64_t per_slot =
+        NV * (1 + 1 + 1 + 4 * 4) + 3 * (NV + 1) * 4 + 4 * 2 * NV * 4 + 4 * (NV / 16) + W * 8 + A * 4 + C * 8;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const int64_t budget = (int64_t)((free_b + (size_t)b->ws_bytes) * 0.5);
     if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
-    if (b->ws && slots == b->ws_slots && N == b->ws_N && W == b->ws_W && A == b->ws_A && C == b->ws_C)
+    if (b->ws && slots == b->ws_slots && N == b->ws_N && W == b->ws_W && A == b->ws_A && C == b->ws_C &&
+        smem_warp == b->P.smem_per_warp)
         return GPSAT_OK;
     cudaFree(b->ws);
     b->ws = nullptr;
@@ -158,11 +177,12 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
         off += (bytes + 255) / 256 * 256;
         return o2;
     };
-    size_t o_val = take(S * N), o_phase = take(S * N), o_seen = take(S * N), o_level = take(S * N * 4),
-           o_reason = take(S * N * 4), o_trail = take(S * N * 4), o_tlim = take(S * (N + 1) * 4),
-           o_learnt = take(S * (N + 1) * 4), o_lstamp = take(S * (N + 1) * 4), o_act = take(S * N * 4),
-           o_ws = take(S * 2 * N * 4), o_wz = take(S * 2 * N * 4), o_wc = take(S * 2 * N * 4),
-           o_wn = take(S * 2 * N * 4), o_w = take(S * W * 8), o_a = take(S * A * 4), o_c = take(S * C * 4),
+    size_t o_val = take(S * NV), o_phase = take(S * NV), o_seen = take(S * NV), o_level = take(S * NV * 4),
+           o_reason = take(S * NV * 4), o_trail = take(S * NV * 4), o_tlim = take(S * (NV + 1) * 4),
+           o_learnt = take(S * (NV + 1) * 4), o_lstamp = take(S * (NV + 1) * 4), o_act = take(S * NV * 4),
+           o_bmax = take(S * (NV / 16) * 4),
+           o_ws = take(S * 2 * NV * 4), o_wz = take(S * 2 * NV * 4), o_wc = take(S * 2 * NV * 4),
+           o_wn = take(S * 2 * NV * 4), o_w = take(S * W * 8), o_a = take(S * A * 4), o_c = take(S * C * 4),
            o_t = take(S * C * 4);
     if (cudaMalloc(&b->ws, off) != cudaSuccess) {
         cudaGetLastError();
@@ -180,6 +200,7 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     P.learnt = (int32_t *)(base + o_learnt);
     P.lstamp = (int32_t *)(base + o_lstamp);
     P.act = (float *)(base + o_act);
+    P.bmax = (float *)(base + o_bmax);
     P.wl_start = (int32_t *)(base + o_ws);
     P.wl_size = (int32_t *)(base + o_wz);
     P.wl_cap = (int32_t *)(base + o_wc);
@@ -190,6 +211,7 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     P.tmp = (int32_t *)(base + o_t);
     P.n_slots = slots;
     P.N = N;
+    P.smem_per_warp = smem_warp;
     P.WCAP = W;
     P.ACAP = A;
     P.CCAP = C;
@@ -462,7 +484,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (J) {
         const int slots = std::min<int32_t>(b->ws_slots, J);
         P.n_slots = slots;
-        cdcl::cdcl_kernel<<<(slots + 3) / 4, 128, 0, st>>>(P);
+        cdcl::cdcl_kernel<<<(slots + 3) / 4, 128, 4 * (size_t)P.smem_per_warp, st>>>(P);
         P.n_slots = b->ws_slots;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_error(err, "solve kernel launch");

@@ -260,6 +260,56 @@ int gpsat_gen_trails(uint64_t seed, int32_t n_vars, int32_t n_trails, double fmi
 int gpsat_gen_planted(uint64_t seed, int32_t n_vars, int64_t n_clauses, int32_t k,
                       int32_t n_communities, double p_in, int32_t *lits, int8_t *planted);
 
+/* ---- learned seeding: message-passing network kernels ----------------------
+ * No counterpart in the reference (it has no learned component): a 3-layer,
+ * 64-wide network over the variable-clause graph whose outputs seed the
+ * solver's VSIDS activities and phases (gpsat_batch_set_seeds) and rank the
+ * JobChooser's split variables.  Matrices are bf16, row-major, 16-byte
+ * aligned, with row strides (ld*) in elements that are multiples of 8;
+ * accumulation is fp32.  All calls are stream ordered and asynchronous;
+ * device pointers only.  An edge is (row << 1) | positive, segments are CSR
+ * (seg_off[segs+1], int64). */
+/* Y[rows x N] = act(X[rows x K] . B^T + bias), B = N x K (row stride ldb),
+ * act = relu when relu != 0; K in {64, 128, 192}, N in {64, 128, 192, 256};
+ * tcgen05 tensor cores.  *err is set to 1 if a tile gave up waiting for its
+ * data or its product. */
+int gpsat_gnn_mm(const void *X, int32_t ldx, int64_t rows, int32_t K, const void *B, int32_t ldb,
+                 int32_t N, const float *bias, int32_t relu, void *Y, int32_t ldy, int32_t *err,
+                 void *stream);
+/* dW[64 x N] += X[rows x 64]^T . dY[rows x N] (fp32 dW, N <= 192, N % 4 == 0) */
+int gpsat_gnn_wgrad(const void *X, int32_t ldx, const void *dY, int32_t ldy, int64_t rows, int32_t N,
+                    float *dW, void *stream);
+/* out[s] = act(seg_scale[s] * sum over edges e of s of (positive ? srcP : srcN)[row e] + Z[s]),
+ * 64 channels; act = relu when relu != 0; seg_scale and Z may be NULL */
+int gpsat_gnn_gather(const int64_t *seg_off, const int32_t *edges, int64_t segs, const void *srcP,
+                     const void *srcN, int32_t lds, const float *seg_scale, const void *Z, int32_t ldz,
+                     void *out, int32_t ldo, int32_t relu, void *stream);
+/* outP[s] / outN[s] = sum of src_scale[row e] * src[row e] over the positive /
+ * negative edges of s (src_scale may be NULL) */
+int gpsat_gnn_gather_split(const int64_t *seg_off, const int32_t *edges, int64_t segs, const void *src,
+                           int32_t lds, const float *src_scale, void *outP, void *outN, int32_t ldo,
+                           void *stream);
+/* dpre = dout where h > 0, else 0 (64 channels) */
+int gpsat_gnn_relu_bwd(const void *dout, int32_t ldd, const void *h, int32_t ldh, int64_t rows, void *dpre,
+                       int32_t ldp, void *stream);
+/* out[64] += column sums of Y (fp32) */
+int gpsat_gnn_colsum(const void *Y, int32_t ldy, int64_t rows, float *out, void *stream);
+/* H[r] = vec (64 fp32 -> bf16) for every row */
+int gpsat_gnn_broadcast(const float *vec, int64_t rows, void *H, int32_t ldh, void *stream);
+/* Heads: score = H.ws + bs, phase = H.wp + bp with head = [ws(64), wp(64), bs, bp].
+ * With y_act != NULL also the losses sum((sigmoid(score) - y_act)^2 * w_act) and
+ * sum(BCE(sigmoid(phase), t_phase) * w_phase) into loss[0..1], their gradient
+ * w.r.t. H into dH and w.r.t. head into ghead (accumulated).  score / phase
+ * outputs may be NULL. */
+int gpsat_gnn_head(const void *H, int32_t ldh, int64_t rows, const float *head, const float *y_act,
+                   const float *w_act, const float *t_phase, const float *w_phase, float *score, float *phase,
+                   void *dH, int32_t ldd, float *ghead, float *loss, void *stream);
+/* Adam step (bias-corrected, step >= 1) on n fp32 parameters; zeroes g. */
+int gpsat_gnn_adam(float *p, float *g, float *m, float *v, int64_t n, float lr, float beta1, float beta2,
+                   float eps, int64_t step, void *stream);
+/* W (K x N fp32) -> fwd = W^T (N x K bf16) and/or bwd = W (K x N bf16, row stride ldb) */
+int gpsat_gnn_pack(const float *W, int32_t K, int32_t N, void *fwd, void *bwd, int32_t ldb, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes
 import json
+import os
 import random
 import sys
 from pathlib import Path
@@ -184,8 +185,39 @@ def solve_cases(stock, nocap):
     print("random n=50 verdicts (nocap):", [r["ref_nocap"] for r in out["random"]])
 
 
+def _nocap_one(args):
+    n, seed = args
+    L = load("nocap")
+    lits, off = g.gen_random_ksat(seed, n, int(round(4.26 * n)), 3)
+    model = np.zeros(n, np.int32)
+    return int(L.ref_solve(P(lits), P(off), n, len(off) - 1, P(model)))
+
+
+def batch_cases():
+    """The reference's verdicts (iteration cap lifted) on the batched-solve
+    workload's instances with n <= 150: instance i of that workload has
+    n = default_rng(11).integers(50, 251, 4096)[i] and formula seed 5000 + i."""
+    import multiprocessing as mp
+    ns = np.random.default_rng(11).integers(50, 251, size=4096)
+    pick = [(int(ns[i]), 5000 + i, i) for i in range(4096) if ns[i] <= 150][:160]
+    out = []
+    with mp.get_context("spawn").Pool(os.cpu_count() or 4) as pool:
+        res = [pool.apply_async(_nocap_one, ((n, seed),)) for n, seed, _ in pick]
+        for (n, seed, i), r in zip(pick, res):
+            try:
+                v = r.get(timeout=120)
+            except mp.TimeoutError:
+                v = None
+            out.append(dict(index=i, seed=seed, n=n, ref_nocap=v))
+    data = json.loads((OUT / "solve_golden.json").read_text())
+    data["batch"] = out
+    (OUT / "solve_golden.json").write_text(json.dumps(data, indent=1))
+    print("batch sample:", len(out), "decided by the reference:", sum(o["ref_nocap"] in (10, 20) for o in out))
+
+
 if __name__ == "__main__":
     stock, nocap = load("stock"), load("nocap")
     bcp_cases(stock)
     preprocess_cases(stock)
     solve_cases(stock, nocap)
+    batch_cases()
