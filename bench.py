@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--impl-cap", type=int, default=4096)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-trails", type=int, default=1024)
+    ap.add_argument("--cpu-trails", type=int, default=4096)
     ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding"],
                     help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
                          "planted: planted community instances split into JobChooser cubes; "
@@ -66,7 +66,10 @@ def parse():
     ap.add_argument("--conflict-budget", type=int, default=100000, help="solve/planted/seeding: per job")
     ap.add_argument("--train-instances", type=int, default=4096, help="seeding: training formulas")
     ap.add_argument("--epochs", type=int, default=3, help="seeding: training passes")
-    ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 1024, seeding: 1024 held-out formulas")
+    ap.add_argument("--train-kind", default="random", choices=["random", "planted"], help="seeding: training set")
+    ap.add_argument("--eval", nargs="+", default=["batch", "random300", "planted"],
+                    choices=["batch", "random300", "planted"], help="seeding: held-out sets (first one is value)")
+    ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 128, seeding: 1024 held-out formulas")
     ap.add_argument("--depth", type=int, default=6, help="planted: split variables per instance (cubes = 2^depth)")
     ap.add_argument("--cpu-instances", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
@@ -160,6 +163,7 @@ def alg_bytes(cnt):
 
 
 def cpu_baseline(lits, off, n, tl, to, ntrails, threads):
+    """The oracle on the first `ntrails` trails with `threads` host threads."""
     import oracle
     o = oracle.BCPOracle(lits, off, n)
     T = min(ntrails, len(to) - 1)
@@ -273,13 +277,16 @@ def run_gpu(args):
     if not args.no_e2e:
         p_tl = torch.from_numpy(tl).pin_memory().numpy()
         p_to = torch.from_numpy(to).pin_memory().numpy()
-        h = b.run_host(p_tl, p_to)  # warm the staging buffers
+        tdt = {np.int32: torch.int32, np.int64: torch.int64}
+        pinned = lambda shape, dt: torch.empty(shape, dtype=tdt[dt], pin_memory=True).numpy()
+        h_out = b.host_outputs(T, counters=True, alloc=pinned)   # reused by every step, as a caller would
+        h = b.run_host(p_tl, p_to, out=h_out)  # warm the staging buffers
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            h = b.run_host(p_tl, p_to)
+            h = b.run_host(p_tl, p_to, out=h_out)
         e2e_s = time.perf_counter() - t0
         if dist:
             t = torch.tensor([e2e_s], device=dev)
@@ -466,43 +473,79 @@ def run_planted_gpu(args):
     print(json.dumps(line))
 
 
+def seeding_eval_set(name, count):
+    """Held-out formulas for the learned-seeding comparison: (formulas, n_vars, communities or None)."""
+    import gpupsat_gb300 as g
+    from gpupsat_gb300 import learn
+    if name == "random300":      # 3-SAT, n = 300, ratio 4.26
+        return [g.gen_random_ksat(40000 + i, 300, 1278, 3) for i in range(count)], [300] * count, None
+    if name == "batch":          # the batched-solve workload's distribution, instances it does not use
+        inst = solve_instances(count, first=8192)
+        return [(l, o) for _, l, o in inst], [n for n, _, _ in inst], None
+    if name == "planted":        # the structured workload's distribution at n ~ U[2000, 5000]
+        ns = np.random.default_rng(17).integers(2000, 5001, size=count)
+        f = [g.gen_planted(70000 + i, int(n), 4 * int(n), 3, 40, 0.9)[:2] for i, n in enumerate(ns)]
+        return f, [int(n) for n in ns], [learn.communities_of(int(n)) for n in ns]
+    raise ValueError(name)
+
+
+def seeding_compare(net, formulas, nv, comm, opts):
+    """Plain and seeded solves of the same formulas; the seeded arm's time
+    includes the network's inference and the seed upload."""
+    import gpupsat_gb300 as g
+    from gpupsat_gb300 import learn
+    bp, bs = g.Batch(formulas, nv), g.Batch(formulas, nv)
+    bp.solve(opts)                                   # warm-up
+    t0 = time.perf_counter()
+    op = bp.solve(opts)
+    plain_s = time.perf_counter() - t0
+    learn.predict(net, formulas, nv, communities=comm)   # warm-up
+    t0 = time.perf_counter()
+    score, phase = learn.predict(net, formulas, nv, communities=comm)
+    bs.set_seeds(*learn.seeds_from(score, phase))
+    infer_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    os_ = bs.solve(opts)
+    seed_s = time.perf_counter() - t0
+    vp, vs = op["verdict"], os_["verdict"]
+    both = (vp != 0) & (vs != 0)
+    assert (vp[both] == vs[both]).all(), "seeded and plain verdicts disagree"
+    assert (op["model_ok"][vp == 10] == 1).all() and (os_["model_ok"][vs == 10] == 1).all()
+    dp, ds = int((vp != 0).sum()), int((vs != 0).sum())
+    return {"instances": len(nv),
+            "plain": {"decided": dp, "decided_per_s": dp / plain_s, "seconds": plain_s,
+                      "median_conflicts": float(np.median(op["stats"][:, 0])),
+                      "mean_conflicts": float(op["stats"][:, 0].mean())},
+            "seeded": {"decided": ds, "decided_per_s": ds / (infer_s + seed_s), "seconds": infer_s + seed_s,
+                       "inference_ms": 1000 * infer_s, "median_conflicts": float(np.median(os_["stats"][:, 0])),
+                       "mean_conflicts": float(os_["stats"][:, 0].mean())}}
+
+
 def run_seeding_gpu(args):
-    """Learned seeding: train the network on budgeted solves of a random k-SAT
-    training set, then solve held-out 3-SAT (n = 300, ratio 4.26) plain and
-    seeded.  value = seeded instances decided/s including the network's
-    inference; the plain arm and the network's own throughput ride along."""
+    """Learned seeding: train the network on budgeted solves of a training set
+    (random k-SAT near threshold, or planted community instances), then solve
+    held-out sets plain and seeded.  value = seeded instances decided/s on the
+    first evaluation set, inference included; every set's plain and seeded
+    figures and the network's forward throughput ride along."""
     import torch
     import gpupsat_gb300 as g
     from gpupsat_gb300 import learn
     torch.cuda.set_device(0)
     dev = torch.device("cuda:0")
     t0 = time.perf_counter()
-    data = learn.training_set(args.train_instances, seed=0)
+    data = learn.training_set(args.train_instances, seed=0, kind=args.train_kind)
     net = learn.SeedNet(dev, seed=0)
     hist, _ = learn.train(net, data, epochs=args.epochs, log=lambda m: print(m, file=sys.stderr))
     train_s = time.perf_counter() - t0
-    held = [(300, *g.gen_random_ksat(40000 + i, 300, 1278, 3)) for i in range(args.instances)]
-    formulas = [(l, o) for _, l, o in held]
-    nv = [n for n, _, _ in held]
-    b = g.Batch(formulas, nv)
     opts = g.solve_options(conflict_budget=args.conflict_budget)
-    out_plain = b.solve(opts)                      # warm-up (and the plain arm's verdicts)
-    t0 = time.perf_counter()
-    out_plain = b.solve(opts)
-    plain_s = time.perf_counter() - t0
-    # seeded: inference + seeds + solve, end to end from the host CNF arrays
-    score, phase = learn.predict(net, formulas, nv)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    score, phase = learn.predict(net, formulas, nv)
-    infer_s = time.perf_counter() - t0
-    act, ph = learn.seeds_from(score, phase)
-    b.set_seeds(act, ph)
-    t0 = time.perf_counter()
-    out_seed = b.solve(opts)
-    seed_solve_s = time.perf_counter() - t0
-    # the network's forward throughput on the held-out graph (device time)
-    G = learn.Graph(formulas, nv, dev)
+    evals = {}
+    for name in args.eval:
+        f, nv, comm = seeding_eval_set(name, args.instances if name != "planted" else max(8, args.instances // 8))
+        evals[name] = seeding_compare(net, f, nv, comm, opts)
+        print(f"{name}: {json.dumps(evals[name])}", file=sys.stderr)
+    # the network's forward throughput on the first evaluation set (device time)
+    f, nv, comm = seeding_eval_set(args.eval[0], args.instances)
+    G = learn.Graph(f, nv, dev, comm)
     ps = learn.Pass(net, G)
     ps.forward()
     torch.cuda.synchronize()
@@ -515,25 +558,18 @@ def run_seeding_gpu(args):
     torch.cuda.synchronize()
     fwd_ms = ev0.elapsed_time(ev1) / reps
     D = learn.D
-    flops = learn.LAYERS * (2 * G.V * D * 3 * D + 2 * G.C * D * D + 2 * G.C * D * 2 * D)
-    vp, vs = out_plain["verdict"], out_seed["verdict"]
-    assert (vp[(vp != 0) & (vs != 0)] == vs[(vp != 0) & (vs != 0)]).all(), "seeded and plain verdicts disagree"
-    assert (out_seed["model_ok"][vs == 10] == 1).all()
-    dec_p, dec_s = int((vp != 0).sum()), int((vs != 0).sum())
-    value = dec_s / (infer_s + seed_solve_s)
-    line = {"metric": "instances decided/s (learned seeding)", "value": value, "unit": "instances/s", "n_gpus": 1,
-            "steps": 1, "warmup": 1, "ms_per_step": 1000 * (infer_s + seed_solve_s), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, int32 solver",
-            "data": "synthetic: seeded random k-SAT (training) and 3-SAT n=300 ratio 4.26 (held out)",
+    flops = 2 * G.V * D * D + learn.LAYERS * (2 * G.V * D * 3 * D + 2 * G.C * D * D + 2 * G.C * D * 2 * D)
+    first = evals[args.eval[0]]
+    line = {"metric": "instances decided/s (learned seeding)", "value": first["seeded"]["decided_per_s"],
+            "unit": "instances/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1000 * first["seeded"]["seconds"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 network, int32 solver",
+            "data": f"synthetic: seeded {args.train_kind} training formulas, held-out sets {args.eval}",
             "config": {"workload": "learned seeding: 3-layer 64-wide message passing, VSIDS + phase seeds",
-                       "train_instances": args.train_instances, "epochs": args.epochs, "held_out": args.instances,
-                       "conflict_budget": args.conflict_budget, "train_seconds": round(train_s, 1),
-                       "final_losses": [round(float(x), 4) for x in hist[-1]]},
-            "plain": {"decided_per_s": dec_p / plain_s, "decided": dec_p,
-                      "median_conflicts": float(np.median(out_plain["stats"][:, 0]))},
-            "seeded": {"decided_per_s": value, "decided": dec_s,
-                       "median_conflicts": float(np.median(out_seed["stats"][:, 0])),
-                       "inference_ms": 1000 * infer_s},
+                       "train_kind": args.train_kind, "train_instances": args.train_instances,
+                       "epochs": args.epochs, "held_out": args.instances, "conflict_budget": args.conflict_budget,
+                       "train_seconds": round(train_s, 1), "final_losses": [round(float(x), 4) for x in hist[-1]]},
+            "evals": evals,
             "network": {"forward_ms": fwd_ms, "tflops": flops / (fwd_ms * 1e-3) / 1e12, "nodes": G.V + G.C,
                         "edges": G.E},
             "gpu_launches": None}
@@ -597,7 +633,7 @@ def run_solve_gpu(args):
 def main():
     args = parse()
     if args.instances is None:
-        args.instances = {"planted": 1024, "seeding": 1024}.get(args.workload, 16384)
+        args.instances = {"planted": 128, "seeding": 1024}.get(args.workload, 16384)
     if args.workload == "seeding":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned seeding; its "

@@ -240,15 +240,33 @@ class BCPBatch:
         check(lib().gpsat_bcp_info(self._h, ctypes.byref(s), ctypes.byref(b)))
         return dict(slots=s.value, device_bytes=b.value)
 
-    def run_host(self, trail_lits: np.ndarray, trail_offsets: np.ndarray, counters: bool = True) -> dict:
+    def host_outputs(self, n_trails: int, counters: bool = True, alloc=np.zeros) -> dict:
+        """Output arrays for run_host (alloc may return pinned memory, e.g. numpy
+        views of torch.empty(..., pin_memory=True))."""
+        T = n_trails
+        return dict(status=alloc(T, np.int32), conflict=alloc(T, np.int32), stop=alloc(T, np.int32),
+                    n_impl=alloc(T, np.int64), impl_lit=alloc((T, self.impl_cap), np.int32),
+                    impl_reason=alloc((T, self.impl_cap), np.int32),
+                    counters=alloc((T, BCP_NCOUNTERS), np.int64) if counters else None)
+
+    def run_host(self, trail_lits: np.ndarray, trail_offsets: np.ndarray, counters: bool = True,
+                 out: dict | None = None) -> dict:
+        """Host buffers in and out (gpsat_bcp_run_host).  `out` (from host_outputs)
+        is reused when given; entries of impl_lit / impl_reason past n_impl[t]
+        are left as they were."""
         trail_lits = np.ascontiguousarray(trail_lits, dtype=np.int32)
         trail_offsets = np.ascontiguousarray(trail_offsets, dtype=np.int64)
         T = len(trail_offsets) - 1
-        out = dict(
-            status=np.empty(T, np.int32), conflict=np.empty(T, np.int32), stop=np.empty(T, np.int32),
-            n_impl=np.empty(T, np.int64), impl_lit=np.zeros((T, self.impl_cap), np.int32),
-            impl_reason=np.zeros((T, self.impl_cap), np.int32),
-            counters=np.zeros((T, BCP_NCOUNTERS), np.int64) if counters else None)
+        if out is None:
+            out = self.host_outputs(T, counters)
+        else:
+            for k, dt in (("status", np.int32), ("conflict", np.int32), ("stop", np.int32), ("n_impl", np.int64),
+                          ("impl_lit", np.int32), ("impl_reason", np.int32)):
+                a = out[k]
+                if a.dtype != dt or a.shape[0] != T or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"run_host: out[{k!r}] must be a contiguous {np.dtype(dt)} array of {T} rows")
+            if out["impl_lit"].shape[1] != self.impl_cap or out["impl_reason"].shape[1] != self.impl_cap:
+                raise ValueError("run_host: implication arrays must have impl_cap columns")
         check(lib().gpsat_bcp_run_host(self._h, _p(trail_lits), _p(trail_offsets), T, _p(out["status"]),
                                        _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
                                        _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out["counters"])))

@@ -19,9 +19,10 @@
 //              (w1<<16)|w2} {first four literals}; each var's entries in the
 //              reference's initial list order
 //   per trail slot (one warp owns one slot; slots are reused across trails)
-//     asg[n]    uint8  (epoch<<1)|sign   trail + pending implications
+//     vr[n]     8 bytes per var: dh  uint32 (epoch<<24)|arena index, head of the
+//               clauses add_first'ed to the var; asg uint8 (epoch<<1)|sign, trail
+//               + pending implications (one load reads both)
 //     cst[m]    uint32 (epoch<<24)|(blocked<<22)|(w1<<11)|w2   clauses touched
-//     dh[n]     uint32 (epoch<<24)|arena index   head of clauses add_first'ed to a var
 //     arena[]   32 bytes per entry: {clause, literal offset, length, next} {literals}
 //     stack[]   int2 depth-first frames (intervals of the implication list)
 //   A slot's epoch (1..127) advances per trail, so nothing is cleared between
@@ -68,15 +69,21 @@ constexpr int64_t MAX_ITERS = int64_t(1) << 26;  // per-trail loop iterations be
 
 enum : int { A_NONE = 0, A_SW1 = 1, A_SW2 = 2, A_BLOCK = 3, A_IMPLY = 4, A_CONFLICT = 5 };
 
+// per-variable record of a trail slot
+struct VarRec {
+    uint32_t dh;       // (epoch<<24)|arena index: head of the clauses add_first'ed to the var
+    uint8_t asg;       // (epoch<<1)|sign: trail literal or pending implication
+    uint8_t pad[3];
+};
+
 struct Dev {
     int32_t n_vars;
     int32_t n_clauses;
     const int32_t *__restrict__ lits;
     const uint32_t *__restrict__ w0off;
     const int4 *__restrict__ w0ent;   // 2 int4 per entry
-    uint8_t *asg;
+    VarRec *vr;
     uint32_t *cst;
-    uint32_t *dh;
     int4 *arena;                      // 2 int4 per entry
     int2 *stack;
     uint32_t *epoch;
@@ -157,12 +164,12 @@ struct Eval {
 
 // process_clause of the reference for a clause too long for the inline path
 // (literals read from the arena).
-__device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const uint32_t *dh, int off, int len,
+__device__ __noinline__ void eval_long(const Dev &d, const VarRec *vr, int off, int len,
                                        int w1, int w2, uint32_t e, Eval &r)
 {
     const int32_t *L = d.lits + off;
     int32_t l1 = L[w1], l2 = L[w2];
-    bool c1 = cons_of(asg[l1 >> 1], l1, e), c2 = cons_of(asg[l2 >> 1], l2, e);
+    bool c1 = cons_of(vr[l1 >> 1].asg, l1, e), c2 = cons_of(vr[l2 >> 1].asg, l2, e);
     r.acnt = 2;
     r.act = A_NONE;
     if (c1 && c2) return;
@@ -171,7 +178,7 @@ __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const u
         if (i == w1 || i == w2) continue;
         int32_t l = L[i];
         r.acnt++;
-        if (cons_of(asg[l >> 1], l, e)) {
+        if (cons_of(vr[l >> 1].asg, l, e)) {
             if (f1 < 0) f1 = i;
             else f2 = i;
             pend--;
@@ -186,7 +193,7 @@ __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const u
             r.nw1 = c1 ? w1 : f1;
             r.nw2 = c1 ? f1 : w2;
             r.t1 = L[f1] >> 1;
-            r.dh1 = dh[r.t1];
+            r.dh1 = vr[r.t1].dh;
             return;
         }
     } else if (f1 >= 0 && f2 >= 0) {
@@ -195,8 +202,8 @@ __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const u
         r.nw2 = f2;
         r.t1 = L[f1] >> 1;
         r.t2 = L[f2] >> 1;
-        r.dh1 = dh[r.t1];
-        r.dh2 = dh[r.t2];
+        r.dh1 = vr[r.t1].dh;
+        r.dh2 = vr[r.t2].dh;
         return;
     } else if (f1 >= 0) {
         unit = L[f1];
@@ -205,7 +212,7 @@ __device__ __noinline__ void eval_long(const Dev &d, const uint8_t *asg, const u
         return;
     }
     r.unit = unit;
-    r.act = ((uint32_t)(asg[unit >> 1] >> 1) != e) ? A_IMPLY : A_BLOCK;
+    r.act = ((uint32_t)(vr[unit >> 1].asg >> 1) != e) ? A_IMPLY : A_BLOCK;
 }
 
 // commit-cut keys: (lane position << 7) | (window scan << 1) | after
@@ -215,9 +222,8 @@ __device__ __forceinline__ int key_after(int pos, int scan) { return ((pos + 1) 
 
 __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int lane)
 {
-    uint8_t *asg = d.asg + (size_t)slot * d.n_pad;
+    VarRec *vr = d.vr + (size_t)slot * d.n_pad;
     uint32_t *cst = d.cst + (size_t)slot * d.m_pad;
-    uint32_t *dh = d.dh + (size_t)slot * d.n_pad;
     int4 *arena = d.arena + (size_t)slot * d.arena_cap * 2;
     int2 *stk = d.stack + (size_t)slot * d.impl_cap;
     int32_t *ilit = d.ilit + (size_t)t * d.impl_cap;
@@ -231,12 +237,10 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     e = __shfl_sync(FULL, e, 0);
     if (e > EPMAX) {
         uint4 z = make_uint4(0, 0, 0, 0);
-        uint4 *a4 = reinterpret_cast<uint4 *>(asg);
-        for (int64_t i = lane; i < d.n_pad / 16; i += 32) a4[i] = z;
+        uint4 *v4 = reinterpret_cast<uint4 *>(vr);
+        for (int64_t i = lane; i < d.n_pad / 2; i += 32) v4[i] = z;
         uint4 *c4 = reinterpret_cast<uint4 *>(cst);
         for (int64_t i = lane; i < d.m_pad / 4; i += 32) c4[i] = z;
-        uint4 *h4 = reinterpret_cast<uint4 *>(dh);
-        for (int64_t i = lane; i < d.n_pad / 4; i += 32) h4[i] = z;
         e = 1;
         __syncwarp();
     }
@@ -250,7 +254,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     for (int64_t i = lane; i < tn; i += 32) {
         int32_t x = d.trail[tb + i];
         if (x == 0 || x > n || x < -n) bad = true;
-        else asg[(x > 0 ? x : -x) - 1] = (uint8_t)((e << 1) | (x > 0 ? 1u : 0u));
+        else vr[(x > 0 ? x : -x) - 1].asg = (uint8_t)((e << 1) | (x > 0 ? 1u : 0u));
     }
     bad = __any_sync(FULL, bad);
     __syncwarp();
@@ -258,7 +262,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         // a variable given both signs leaves one of its literals unmatched
         for (int64_t i = lane; i < tn; i += 32) {
             int32_t x = d.trail[tb + i];
-            if (asg[(x > 0 ? x : -x) - 1] != (uint8_t)((e << 1) | (x > 0 ? 1u : 0u))) bad = true;
+            if (vr[(x > 0 ? x : -x) - 1].asg != (uint8_t)((e << 1) | (x > 0 ? 1u : 0u))) bad = true;
         }
         bad = __any_sync(FULL, bad);
     }
@@ -326,7 +330,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                     cur_wend = d.w0off[v + 1];
                 }
             }
-            uint32_t h = dh[v];
+            uint32_t h = vr[v].dh;
             cur_var = v;
             cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
             if (!cur_is_trail) {
@@ -498,10 +502,12 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             // literals' assignments and list heads (unused ones are cheap misses)
 #pragma unroll
             for (int i = 0; i < KIN; i++) {
-                Av[i] = (i < len) ? asg[Lr[i] >> 1] : 0;
-                Dh[i] = (i < len) ? dh[Lr[i] >> 1] : 0;
+                // one 8-byte load per literal: list head and assignment byte
+                const uint2 rv = (i < len) ? *reinterpret_cast<const uint2 *>(&vr[Lr[i] >> 1]) : make_uint2(0, 0);
+                Av[i] = (uint8_t)(rv.y & 0xFFu);
+                Dh[i] = rv.x;
             }
-            if (scan_v >= 0) scan_h = dh[scan_v];
+            if (scan_v >= 0) scan_h = vr[scan_v].dh;
             bool blk;
             if ((st >> 24) == e) {
                 blk = (st >> 22) & 1u;
@@ -591,10 +597,10 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             } else {
                 const int32_t l1 = d.lits[en.y + w1], l2 = d.lits[en.y + w2];
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
-                if (valid) eval_long(d, asg, dh, en.y, len, w1, w2, e, r);
+                if (valid) eval_long(d, vr, en.y, len, w1, w2, e, r);
             }
         } else if (scan_v >= 0) {
-            scan_h = dh[scan_v];
+            scan_h = vr[scan_v].dh;
         }
 
         // ---- where the commit stops: the smallest event key of the round
@@ -696,7 +702,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 }
                 arena[2 * myidx] = make_int4(en.x, en.y, en.z, next);
                 arena[2 * myidx + 1] = el;
-                if ((g & lanemask_gt()) == 0) dh[r.t1] = (e << 24) | (uint32_t)myidx;
+                if ((g & lanemask_gt()) == 0) vr[r.t1].dh = (e << 24) | (uint32_t)myidx;
             }
         } else {
             // rare (a clause moving both watches needs 4+ literals): lane 0
@@ -713,17 +719,17 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 const int32_t tt1 = __shfl_sync(FULL, r.t1, k), tt2 = __shfl_sync(FULL, r.t2, k);
                 const bool two = (m2 >> k) & 1u;
                 if (lane == 0) {
-                    uint32_t h = dh[tt1];
+                    uint32_t h = vr[tt1].dh;
                     int32_t next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
                     arena[2 * idx] = make_int4(c, off, len, next);
                     arena[2 * idx + 1] = lk;
-                    dh[tt1] = (e << 24) | (uint32_t)idx;
+                    vr[tt1].dh = (e << 24) | (uint32_t)idx;
                     if (two) {
-                        h = dh[tt2];
+                        h = vr[tt2].dh;
                         next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
                         arena[2 * (idx + 1)] = make_int4(c, off, len, next);
                         arena[2 * (idx + 1) + 1] = lk;
-                        dh[tt2] = (e << 24) | (uint32_t)(idx + 1);
+                        vr[tt2].dh = (e << 24) | (uint32_t)(idx + 1);
                     }
                 }
                 idx += two ? 2 : 1;
@@ -744,7 +750,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 const int64_t at = n_impl + __popc(imask & lt);
                 ilit[at] = dimacs_of(r.unit);
                 ireason[at] = en.x;
-                asg[r.unit >> 1] = (uint8_t)((e << 1) | (uint32_t)(r.unit & 1));
+                vr[r.unit >> 1].asg = (uint8_t)((e << 1) | (uint32_t)(r.unit & 1));
             }
             n_impl += __popc(imask);
             cI += __popc(imask);
@@ -775,7 +781,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             if (!new_started) {
                 // cut before this scan because its list starts with added
                 // clauses (possibly added by this round): those come first
-                const uint32_t h = dh[cur_var];
+                const uint32_t h = vr[cur_var].dh;
                 cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
             }
             cur_wk = sm.sc_wk[new_cur] + (uint32_t)(k_end - sm.sc_begin[new_cur]);
@@ -852,8 +858,8 @@ struct gpsat_bcp {
     int device = 0;
     int32_t slots = 0;
     int64_t n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
-    uint8_t *asg = nullptr;
-    uint32_t *cst = nullptr, *dh = nullptr, *epoch = nullptr;
+    bcp::VarRec *vr = nullptr;
+    uint32_t *cst = nullptr, *epoch = nullptr;
     int4 *arena = nullptr;
     int2 *stack = nullptr;
     unsigned int *counter = nullptr;
@@ -870,9 +876,8 @@ namespace {
 
 void bcp_free(gpsat_bcp *b)
 {
-    cudaFree(b->asg);
+    cudaFree(b->vr);
     cudaFree(b->cst);
-    cudaFree(b->dh);
     cudaFree(b->epoch);
     cudaFree(b->arena);
     cudaFree(b->stack);
@@ -893,9 +898,8 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
     d.lits = f->d_lits;
     d.w0off = f->d_w0off;
     d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
-    d.asg = b->asg;
+    d.vr = b->vr;
     d.cst = b->cst;
-    d.dh = b->dh;
     d.arena = b->arena;
     d.stack = b->stack;
     d.epoch = b->epoch;
@@ -951,7 +955,7 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
     b->m_pad = (f->h.n_clauses() + 3) / 4 * 4;
     b->impl_cap = impl_cap;
     b->arena_cap = arena_cap ? arena_cap : (1 << 17);
-    const int64_t per_slot = b->n_pad * 5 + b->m_pad * 4 + b->arena_cap * 32 + b->impl_cap * 8;
+    const int64_t per_slot = b->n_pad * 8 + b->m_pad * 4 + b->arena_cap * 32 + b->impl_cap * 8;
     int32_t slots = max_slots ? max_slots : resident;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -959,17 +963,15 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
     if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
     b->slots = slots;
     const size_t S = (size_t)slots;
-    bool ok = cudaMalloc(&b->asg, S * b->n_pad) == cudaSuccess &&
+    bool ok = cudaMalloc(&b->vr, S * b->n_pad * 8) == cudaSuccess &&
               cudaMalloc(&b->cst, S * b->m_pad * 4) == cudaSuccess &&
-              cudaMalloc(&b->dh, S * b->n_pad * 4) == cudaSuccess &&
               cudaMalloc(&b->epoch, S * 4) == cudaSuccess &&
               cudaMalloc(&b->arena, S * b->arena_cap * 32) == cudaSuccess &&
               cudaMalloc(&b->stack, S * b->impl_cap * 8) == cudaSuccess &&
               cudaMalloc(&b->counter, 16) == cudaSuccess;
     if (ok)
-        ok = cudaMemset(b->asg, 0, S * b->n_pad) == cudaSuccess &&
-             cudaMemset(b->cst, 0, S * b->m_pad * 4) == cudaSuccess &&
-             cudaMemset(b->dh, 0, S * b->n_pad * 4) == cudaSuccess && cudaMemset(b->epoch, 0, S * 4) == cudaSuccess;
+        ok = cudaMemset(b->vr, 0, S * b->n_pad * 8) == cudaSuccess &&
+             cudaMemset(b->cst, 0, S * b->m_pad * 4) == cudaSuccess && cudaMemset(b->epoch, 0, S * 4) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         bcp_free(b);
@@ -1110,7 +1112,7 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
 // and hosts whose device memory is reserved up front by their own pool.  The
 // call below makes no allocating CUDA call and no library allocation; the
 // slots' state lives in bcp_static_scratch, laid out afresh by every call:
-//   [launch counter | epoch per slot | asg | cst | dh | move arena | stack]
+//   [launch counter | epoch per slot | variable records | cst | move arena | stack]
 // each part 256-byte aligned.  Everything but the arena and the stack (which
 // the kernel writes before it reads) is cleared on the stream per call.  One
 // array per device, so calls whose GPU work overlaps race on it.
@@ -1172,8 +1174,8 @@ int static_setup(int device, unsigned char **base, int32_t *resident)
 // Bytes of the scratch layout for S slots (each part rounded up to 256).
 int64_t static_layout_bytes(int64_t S, int64_t n_pad, int64_t m_pad, int64_t arena_cap, int64_t impl_cap)
 {
-    return STATIC_ALIGN + align_up(S * 4) + align_up(S * n_pad) + align_up(S * m_pad * 4) +
-           align_up(S * n_pad * 4) + align_up(S * arena_cap * 32) + align_up(S * impl_cap * 8);
+    return STATIC_ALIGN + align_up(S * 4) + align_up(S * n_pad * 8) + align_up(S * m_pad * 4) +
+           align_up(S * arena_cap * 32) + align_up(S * impl_cap * 8);
 }
 
 }  // namespace
@@ -1216,7 +1218,7 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
         return set_error(GPSAT_ERR_CAPACITY, msg);
     }
     int64_t S = std::min<int64_t>(resident, std::max<int32_t>(n_trails, 1));
-    const int64_t per_slot = 4 + n_pad * 5 + m_pad * 4 + acap * 32 + impl_cap * 8;
+    const int64_t per_slot = 4 + n_pad * 8 + m_pad * 4 + acap * 32 + impl_cap * 8;
     S = std::min<int64_t>(S, std::max<int64_t>(1, (limit - 7 * STATIC_ALIGN) / per_slot));
     while (S > 1 && static_layout_bytes(S, n_pad, m_pad, acap, impl_cap) > limit) S--;
 
@@ -1228,9 +1230,8 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     };
     unsigned int *counter = reinterpret_cast<unsigned int *>(take(STATIC_ALIGN));
     uint32_t *epoch = reinterpret_cast<uint32_t *>(take(S * 4));
-    uint8_t *asg = take(S * n_pad);
+    bcp::VarRec *vr = reinterpret_cast<bcp::VarRec *>(take(S * n_pad * 8));
     uint32_t *cst = reinterpret_cast<uint32_t *>(take(S * m_pad * 4));
-    uint32_t *dh = reinterpret_cast<uint32_t *>(take(S * n_pad * 4));
     int4 *arena = reinterpret_cast<int4 *>(take(S * acap * 32));
     int2 *stack = reinterpret_cast<int2 *>(take(S * impl_cap * 8));
 
@@ -1240,9 +1241,8 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     // another formula with another layout)
     err = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
     if (err == cudaSuccess) err = cudaMemsetAsync(epoch, 0, (size_t)S * 4, st);
-    if (err == cudaSuccess) err = cudaMemsetAsync(asg, 0, (size_t)(S * n_pad), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(vr, 0, (size_t)(S * n_pad * 8), st);
     if (err == cudaSuccess) err = cudaMemsetAsync(cst, 0, (size_t)(S * m_pad * 4), st);
-    if (err == cudaSuccess) err = cudaMemsetAsync(dh, 0, (size_t)(S * n_pad * 4), st);
     if (err != cudaSuccess) return cuda_error(err, "gpsat_bcp_run_static: clearing the static scratch");
     if (n_trails == 0) return GPSAT_OK;
 
@@ -1252,9 +1252,8 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     d.lits = f->d_lits;
     d.w0off = f->d_w0off;
     d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
-    d.asg = asg;
+    d.vr = vr;
     d.cst = cst;
-    d.dh = dh;
     d.arena = arena;
     d.stack = stack;
     d.epoch = epoch;

@@ -87,6 +87,7 @@ struct Ctx {
     float *act;
     float *bmax;     // per block of 32 variables: >= the largest activity of its unassigned
                      // variables (-1: none left); exact for a block pick_branch last tightened
+    bool use_bmax;   // large formulas pick through the block bounds, small ones scan
     int32_t *wl_start, *wl_size, *wl_cap, *wl_cnt;
     int2 *watches;
     int32_t *arena, *crefs;
@@ -302,11 +303,23 @@ __device__ int32_t propagate(Ctx &C)
                 if (v0 == 1) {
                     blk = l0;
                 } else {
-                    int k = 2;
+                    // first literal at position >= 2 that is not false, four
+                    // literals per 16-byte load (chunks aligned in the arena,
+                    // whose slot base and capacity are multiples of 4 words)
+                    int k = len;
                     int32_t lk = 0;
-                    for (; k < len; k++) {
-                        lk = CL[k];
-                        if (lval(C, lk) != -1) break;
+                    const int64_t a0 = (int64_t)w.x + HDR + 2, a1 = (int64_t)w.x + HDR + len;
+                    for (int64_t c = a0 & ~int64_t(3); c < a1 && k == len; c += 4) {
+                        const int4 q = *reinterpret_cast<const int4 *>(C.arena + c);
+                        const int32_t qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int64_t at = c + j;
+                            if (k == len && at >= a0 && at < a1 && lval(C, qq[j]) != -1) {
+                                k = (int)(at - ((int64_t)w.x + HDR));
+                                lk = qq[j];
+                            }
+                        }
                     }
                     blk = l0;
                     if (k < len) {
@@ -420,7 +433,7 @@ __device__ int32_t propagate(Ctx &C)
 // bits raises a block bound.
 __device__ __forceinline__ void raise_bound(Ctx &C, int32_t v, float a)
 {
-    atomicMax(reinterpret_cast<int *>(&C.bmax[v >> 5]), __float_as_int(a));
+    if (C.use_bmax) atomicMax(reinterpret_cast<int *>(&C.bmax[v >> 5]), __float_as_int(a));
 }
 
 __device__ __forceinline__ void bump(Ctx &C, int32_t v, bool &big)
@@ -434,8 +447,9 @@ __device__ __forceinline__ void bump(Ctx &C, int32_t v, bool &big)
 __device__ void rescale(Ctx &C)
 {
     for (int v = C.lane; v < C.n; v += 32) C.act[v] *= 1e-30f;
-    for (int b = C.lane; b < (C.n + 31) / 32; b += 32)
-        if (C.bmax[b] >= 0.f) C.bmax[b] *= 1e-30f;
+    if (C.use_bmax)
+        for (int b = C.lane; b < (C.n + 31) / 32; b += 32)
+            if (C.bmax[b] >= 0.f) C.bmax[b] *= 1e-30f;
     C.var_inc *= 1e-30f;
     __syncwarp();
 }
@@ -742,7 +756,31 @@ __device__ int32_t pick_branch(Ctx &C, int mode)
         return best < 0 ? -1 : 2 * best + 1;
     }
     // VSIDS: the unassigned variable of largest activity, lowest index on ties.
-    // Take the block with the largest bound (lowest block on ties), compute its
+    if (!C.use_bmax) {
+        // small formulas: one warp scan over every variable
+        float ba = -FLT_MAX;
+        int bv = -1;
+        for (int v = lane; v < C.n; v += 32) {
+            if (C.val[v] == 0) {
+                const float a = C.act[v];
+                if (bv < 0 || a > ba) {
+                    ba = a;
+                    bv = v;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(FULL, ba, o);
+            const int ov = __shfl_xor_sync(FULL, bv, o);
+            if (ov >= 0 && (bv < 0 || oa > ba || (oa == ba && ov < bv))) {
+                ba = oa;
+                bv = ov;
+            }
+        }
+        return bv < 0 ? -1 : 2 * bv + (C.phase[bv] ? 1 : 0);
+    }
+    // Large formulas: take the block with the largest bound (lowest block on ties), compute its
     // exact best; if that reaches the bound it beats every other block, else
     // tighten the bound and look again.  Every round either answers or makes one
     // bound exact, so the loop ends; the answer is the full scan's.
@@ -840,8 +878,9 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
         C.phase[v] = P.seed_phase ? P.seed_phase[voff + v] : (int8_t)o.phase_init;
     }
     for (int v = lane; v <= C.n; v += 32) C.lstamp[v] = 0;
+    C.use_bmax = C.n > 1024;
     __syncwarp();
-    for (int b = lane; b < (C.n + 31) / 32; b += 32) {
+    for (int b = lane; C.use_bmax && b < (C.n + 31) / 32; b += 32) {
         float x = 0.f;
         for (int v = 32 * b; v < 32 * b + 32 && v < C.n; v++) x = fmaxf(x, C.act[v]);
         C.bmax[b] = x;

@@ -135,7 +135,9 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     const int32_t N = (int32_t)((*std::max_element(b->n_vars.begin(), b->n_vars.end()) + 15) / 16 * 16);
     const int64_t lfirst = std::max<int64_t>(o->learnt_first, b->max_m / 2);
     const int64_t C = b->max_m + 3 * lfirst + 4 * (int64_t)o->learnt_inc + N + 64;
-    const int64_t A = b->max_words + (C - b->max_m) * 48;
+    // a multiple of 4 words: every slot's arena starts 16-byte aligned (the
+    // replacement-watch search reads clause literals four at a time)
+    const int64_t A = (b->max_words + (C - b->max_m) * 48 + 3) / 4 * 4;
     const int64_t W = 3 * C + 8 * (int64_t)N + 256;
     int sms = 0, per_sm = 0, smem_max = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);

@@ -341,27 +341,49 @@ def train_step(net: SeedNet, formulas, n_vars, y, t, has_phase, lr=1e-3, stream=
 
 
 # ---------------------------------------------------------------- workloads
-def training_set(count: int, seed: int = 0):
-    """Random k-SAT near the satisfiability thresholds: k in {3, 4, 5} with
-    clause ratios 4.26 / 9.93 / 21.1, n ~ U[100, 400]; formula i uses
-    generator seed 20000 + seed * 1000003 + i."""
-    from . import gen_random_ksat
+def communities_of(n: int, groups: int = 40) -> np.ndarray:
+    """Community id of each variable of a planted instance (equal contiguous blocks)."""
+    return (np.arange(n, dtype=np.int64) * groups // n).astype(np.float32)
+
+
+def training_set(count: int, seed: int = 0, kind: str = "random"):
+    """Training formulas as (n, lits, offsets, communities or None).
+
+    "random":  random k-SAT near the satisfiability thresholds, k in {3, 4, 5}
+               with clause ratios 4.26 / 9.93 / 21.1, n ~ U[100, 400]; formula i
+               uses generator seed 20000 + seed * 1000003 + i.
+    "planted": planted community 3-SAT as the structured workload generates it
+               (ratio 4.0, 40 communities, 90% of a clause in one), smaller:
+               n ~ U[500, 3000]; formula i uses seed 60000 + seed * 1000003 + i.
+    """
+    from . import gen_planted, gen_random_ksat
     rng = np.random.default_rng(seed)
-    ks = rng.choice([3, 4, 5], size=count)
-    ns = rng.integers(100, 401, size=count)
-    ratio = {3: 4.26, 4: 9.93, 5: 21.1}
     out = []
-    for i, (k, n) in enumerate(zip(ks, ns)):
-        lits, off = gen_random_ksat(20000 + seed * 1000003 + i, int(n), int(round(ratio[int(k)] * n)), int(k))
-        out.append((int(n), lits, off))
+    if kind == "random":
+        ks = rng.choice([3, 4, 5], size=count)
+        ns = rng.integers(100, 401, size=count)
+        ratio = {3: 4.26, 4: 9.93, 5: 21.1}
+        for i, (k, n) in enumerate(zip(ks, ns)):
+            lits, off = gen_random_ksat(20000 + seed * 1000003 + i, int(n), int(round(ratio[int(k)] * n)), int(k))
+            out.append((int(n), lits, off, None))
+    elif kind == "planted":
+        ns = rng.integers(500, 3001, size=count)
+        for i, n in enumerate(ns):
+            lits, off, _ = gen_planted(60000 + seed * 1000003 + i, int(n), 4 * int(n), 3, 40, 0.9)
+            out.append((int(n), lits, off, communities_of(int(n))))
+    else:
+        raise ValueError(f"unknown training set {kind!r}")
     return out
 
 
 def train(net: SeedNet, data, epochs: int = 3, batch: int = 256, lr: float = 2e-3, conflict_budget: int = 20000,
           log=print):
-    """Labels every formula with the solver, then trains for `epochs` passes."""
-    formulas = [(l, o) for _, l, o in data]
-    nv = [n for n, _, _ in data]
+    """Labels every formula with the solver, then trains for `epochs` passes.
+    data: (n, lits, offsets[, communities]) tuples."""
+    formulas = [(d[1], d[2]) for d in data]
+    nv = [d[0] for d in data]
+    comm = [d[3] if len(d) > 3 else None for d in data]
+    use_comm = any(c is not None for c in comm)
     y, t, has_phase, out = participation_targets(formulas, nv, conflict_budget)
     base = np.zeros(len(nv) + 1, np.int64)
     base[1:] = np.cumsum(nv)
@@ -373,8 +395,9 @@ def train(net: SeedNet, data, epochs: int = 3, batch: int = 256, lr: float = 2e-
         for b0 in range(0, len(order), batch):
             idx = order[b0:b0 + batch]
             sel = np.concatenate([np.arange(base[i], base[i + 1]) for i in idx])
+            cm = [comm[i] if comm[i] is not None else np.zeros(nv[i], np.float32) for i in idx] if use_comm else None
             la, lp = train_step(net, [formulas[i] for i in idx], [nv[i] for i in idx], y[sel], t[sel],
-                                has_phase[sel], lr=lr)
+                                has_phase[sel], lr=lr, communities=cm)
             tot += (la, lp)
         nb = (len(order) + batch - 1) // batch
         hist.append(tot / nb)

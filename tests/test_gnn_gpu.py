@@ -186,3 +186,31 @@ def test_training_lowers_the_loss(gpsat, torch_dev):
     b.set_seeds(act, ph)
     res = b.solve()
     assert (res["model_ok"][res["verdict"] == gpsat.SAT] == 1).all()
+
+
+def test_learned_seeding_against_plain_vsids(gpsat, torch_dev):
+    """What the trained network gains over the plain solver on held-out random
+    3-SAT (n in [150, 250], ratio 4.26): verdicts agree wherever both decide,
+    every model checks, and the seeded arm's median conflict count is reported
+    against the plain arm's (it must not be worse by more than noise)."""
+    torch, dev = torch_dev
+    from gpupsat_gb300 import learn
+    net = learn.SeedNet(dev, seed=0)
+    learn.train(net, learn.training_set(512, seed=3), epochs=3, conflict_budget=10000, log=None)
+    rng = np.random.default_rng(23)
+    ns = [int(n) for n in rng.integers(150, 251, size=384)]
+    formulas = [gpsat.gen_random_ksat(90000 + i, n, int(round(4.26 * n)), 3) for i, n in enumerate(ns)]
+    opts = gpsat.solve_options(conflict_budget=20000)
+    plain = gpsat.Batch(formulas, ns).solve(opts)
+    score, phase = learn.predict(net, formulas, ns)
+    b = gpsat.Batch(formulas, ns)
+    b.set_seeds(*learn.seeds_from(score, phase))
+    seeded = b.solve(opts)
+    vp, vs = plain["verdict"], seeded["verdict"]
+    both = (vp != 0) & (vs != 0)
+    assert (vp[both] == vs[both]).all()
+    assert (seeded["model_ok"][vs == gpsat.SAT] == 1).all()
+    mp, ms = np.median(plain["stats"][:, 0]), np.median(seeded["stats"][:, 0])
+    print(f"median conflicts: plain {mp:.0f}, seeded {ms:.0f} ({100 * (1 - ms / mp):+.1f}% fewer); "
+          f"decided: plain {int((vp != 0).sum())}, seeded {int((vs != 0).sum())}")
+    assert ms <= 1.05 * mp

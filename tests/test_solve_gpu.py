@@ -110,3 +110,16 @@ def test_conflict_budget_gives_unknown(gpsat, cuda_ok):
     out = b.solve(gpsat.solve_options(conflict_budget=5))
     assert out["verdict"][0] == gpsat.UNKNOWN
     assert out["stats"][0, 7] & 4
+
+
+def test_batched_workload_sample_matches_reference(gpsat, cuda_ok, solve_golden):
+    """Instances of the batched-solve workload with n <= 150 (the first 160 of
+    them), against the reference's own verdicts with its iteration cap lifted."""
+    rs = solve_golden["batch"]
+    formulas = [gpsat.gen_random_ksat(r["seed"], r["n"], int(round(4.26 * r["n"])), 3) for r in rs]
+    out = solve_all(gpsat, formulas, [r["n"] for r in rs])
+    assert (out["verdict"] != 0).all()
+    decided = [(r, int(v)) for r, v in zip(rs, out["verdict"]) if r["ref_nocap"] in (10, 20)]
+    assert len(decided) >= 150
+    bad = [(r["index"], r["ref_nocap"], v) for r, v in decided if r["ref_nocap"] != v]
+    assert not bad, f"verdicts differ from the reference: {bad[:5]}"
