@@ -70,7 +70,8 @@ def parse():
     ap.add_argument("--eval", nargs="+", default=["batch", "random300", "planted"],
                     choices=["batch", "random300", "planted"], help="seeding: held-out sets (first one is value)")
     ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 128, seeding: 1024 held-out formulas")
-    ap.add_argument("--depth", type=int, default=6, help="planted: split variables per instance (cubes = 2^depth)")
+    ap.add_argument("--depth", default="6", help="planted: split variables per instance (cubes = 2^depth), "
+                                                 "or 'auto' to autotune it on a sample")
     ap.add_argument("--cpu-instances", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     return ap.parse_args()
@@ -428,8 +429,15 @@ def run_planted_gpu(args):
     inst = planted_instances(args.instances)
     formulas = [(l, o) for _, l, o in inst]
     nv = [n for n, _, _ in inst]
-    jf, co, cl = jobs.cube_jobs(formulas, nv, args.depth)
     opts = g.solve_options(conflict_budget=args.conflict_budget)
+    tuned = None
+    if args.depth == "auto":
+        depth, table = jobs.autotune_depth(formulas, nv, depths=(4, 6, 8, 10), sample=16, options=opts,
+                                           log=lambda m: print(m, file=sys.stderr))
+        tuned = {str(d): {"decided": t[0], "seconds": round(t[1], 3)} for d, t in table.items()}
+    else:
+        depth = int(args.depth)
+    jf, co, cl = jobs.cube_jobs(formulas, nv, depth)
     b = g.Batch(formulas, nv)
     for _ in range(args.warmup):
         out = b.solve(opts, jobs=(jf, co, cl))
@@ -460,7 +468,8 @@ def run_planted_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded planted 3-SAT with 40 communities",
             "config": {"workload": "structured batch: planted community 3-SAT, n ~ U[2000,20000], m = 4.0 n",
-                       "instances": args.instances, "cube_depth": args.depth, "jobs": int(len(jf)),
+                       "instances": args.instances, "cube_depth": depth, "depth_autotune": tuned,
+                       "jobs": int(len(jf)),
                        "chooser": "MaxClauseJobChooser ranking (reference VariableChooser score)",
                        "l2": "per-job state > L2; no flush needed"},
             "cpu_baseline": None, "clocks": clk,

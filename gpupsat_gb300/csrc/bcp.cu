@@ -251,6 +251,8 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
 
     // ---- assign every trail literal first
     bool bad = tn < 0;
+    // (unrolled so that several iterations' loads are in flight at once)
+#pragma unroll 4
     for (int64_t i = lane; i < tn; i += 32) {
         int32_t x = d.trail[tb + i];
         if (x == 0 || x > n || x < -n) bad = true;
@@ -260,6 +262,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     __syncwarp();
     if (!bad) {
         // a variable given both signs leaves one of its literals unmatched
+#pragma unroll 4
         for (int64_t i = lane; i < tn; i += 32) {
             int32_t x = d.trail[tb + i];
             if (vr[(x > 0 ? x : -x) - 1].asg != (uint8_t)((e << 1) | (x > 0 ? 1u : 0u))) bad = true;
@@ -413,10 +416,13 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                     lb_a = d.w0off[lb_v];
                     lb_b = d.w0off[lb_v + 1];
                     // warm L2 with these scans' initial watch entries (up to 32
-                    // each, four 32-byte entries per line): the rounds of the
-                    // next 16-32 trail scans gather them
-                    for (uint32_t w = lb_a; w < lb_b && w < lb_a + 32; w += 4)
-                        asm volatile("prefetch.L2 [%0];" ::"l"(d.w0ent + 2 * (size_t)w));
+                    // each) by one bulk prefetch of the copy engine per scan:
+                    // the rounds of the next 16-32 trail scans gather them
+                    const uint32_t ne = lb_b - lb_a < 32u ? lb_b - lb_a : 32u;
+                    if (ne > 0)
+                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(d.w0ent + 2 * (size_t)lb_a),
+                                     "r"(ne * 32u)
+                                     : "memory");
                 }
             }
             const int lb_off = (int)(ti - lb_base);
@@ -1197,7 +1203,11 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
         return set_error(GPSAT_ERR_STATE,
                          "gpsat_bcp_run_static: the formula is not on the device yet (gpsat_bcp_create on it "
                          "uploads it; this entry point allocates nothing, so it cannot upload)");
-    cudaError_t err = cudaSetDevice(f->device);
+    // switch devices only when needed: a caller capturing this call into a
+    // graph keeps its device current
+    int cur_dev = -1;
+    cudaError_t err = cudaGetDevice(&cur_dev);
+    if (err == cudaSuccess && cur_dev != f->device) err = cudaSetDevice(f->device);
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
     unsigned char *base = nullptr;
     int32_t resident = 0;

@@ -287,6 +287,15 @@ __device__ int32_t propagate(Ctx &C)
                 fail_check(C, CK_CREF);
                 return -1;
             }
+            // every watch of the batch has a true blocker: it stays as it is
+            // (moved down over the entries earlier batches moved away)
+            if (__all_sync(FULL, !has || lval(C, w.y) == 1)) {
+                if (j != i && has) C.watches[s + j + lane] = w;
+                j += cnt;
+                i += cnt;
+                __syncwarp();
+                continue;
+            }
             int act = W_KEEP;
             int32_t blk = w.y, imp = -1, tgt = -1, l0 = 0;
             int kpos = -1;
@@ -361,12 +370,15 @@ __device__ int32_t propagate(Ctx &C)
             // several lanes may imply the same variable: the lowest lane wins,
             // the same literal again is kept, the opposite one is a conflict
             const bool is_imp = act == W_IMPLY;
-            const int32_t key = is_imp ? (imp >> 1) : -1 - lane;
-            const unsigned grp = __match_any_sync(FULL, key);
-            const int lead = __ffs(grp) - 1;
-            const int32_t lead_lit = __shfl_sync(FULL, imp, lead);
-            const bool winner = is_imp && lead == lane;
-            if (is_imp && !winner) act = (imp == lead_lit) ? W_KEEP : W_CONFL;
+            bool winner = false;
+            if (__any_sync(FULL, is_imp)) {
+                const int32_t key = is_imp ? (imp >> 1) : -1 - lane;
+                const unsigned grp = __match_any_sync(FULL, key);
+                const int lead = __ffs(grp) - 1;
+                const int32_t lead_lit = __shfl_sync(FULL, imp, lead);
+                winner = is_imp && lead == lane;
+                if (is_imp && !winner) act = (imp == lead_lit) ? W_KEEP : W_CONFL;
+            }
             const unsigned wm = __ballot_sync(FULL, winner);
             if (C.tsize + __popc(wm) > C.n) {  // more assignments than variables
                 fail_check(C, CK_TRAIL);
@@ -1048,7 +1060,7 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
     return result;
 }
 
-__global__ void __launch_bounds__(WARPS * 32) cdcl_kernel(Params P)
+__device__ __forceinline__ void cdcl_body(const Params &P)
 {
     __shared__ int32_t smem[WARPS][64];
     extern __shared__ __align__(16) unsigned char dyn_smem[];
@@ -1137,6 +1149,12 @@ __global__ void __launch_bounds__(WARPS * 32) cdcl_kernel(Params P)
         __syncwarp();
     }
 }
+
+// Two register targets: 4 blocks/SM (128 registers) when the per-variable
+// arrays sit in HBM, 3 (about 160) when they sit in shared memory, which four
+// blocks of N > 240 variables would not fit.
+__global__ void __launch_bounds__(WARPS * 32, 3) cdcl_kernel_smem(Params P) { cdcl_body(P); }
+__global__ void __launch_bounds__(WARPS * 32, 4) cdcl_kernel_hbm(Params P) { cdcl_body(P); }
 
 }  // namespace cdcl
 }  // namespace gpsat

@@ -24,7 +24,8 @@
 
 namespace gpsat {
 namespace cdcl {
-__global__ void cdcl_kernel(Params P);
+__global__ void cdcl_kernel_smem(Params P);
+__global__ void cdcl_kernel_hbm(Params P);
 }
 
 namespace {
@@ -99,7 +100,7 @@ struct gpsat_batch {
     // workspace
     cdcl::Params P{};
     int64_t ws_bytes = 0;
-    int32_t ws_slots = 0, ws_N = 0;
+    int32_t ws_slots = 0, ws_N = 0, minb = 3;
     int64_t ws_W = 0, ws_A = 0, ws_C = 0;
     void *ws = nullptr;
     int max_len = 0, max_m = 0;
@@ -142,21 +143,27 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     int sms = 0, per_sm = 0, smem_max = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel, 128, 0);
-    // the per-variable arrays go to shared memory when that costs no
-    // resident warps (the kernel's registers already cap the blocks per SM)
+    // Two builds of the kernel: 3 blocks/SM with the per-variable arrays in
+    // shared memory when three blocks of them fit (no fewer resident blocks
+    // than its registers allow), else 4 blocks/SM with them in HBM.
     int32_t smem_warp = (int32_t)cdcl::smem_bytes_per_warp(N);
+    int minb = 3;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel_smem, 128, 0);
     if (4 * (int64_t)smem_warp + 1024 > smem_max) smem_warp = 0;
     if (smem_warp > 0) {
         int per_sm_smem = 0;
-        if (cudaFuncSetAttribute(cdcl::cdcl_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * smem_warp) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_smem, cdcl::cdcl_kernel, 128, 4 * smem_warp) !=
+        if (cudaFuncSetAttribute(cdcl::cdcl_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 4 * smem_warp) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_smem, cdcl::cdcl_kernel_smem, 128, 4 * smem_warp) !=
                 cudaSuccess ||
             per_sm_smem < per_sm) {
             cudaGetLastError();
             smem_warp = 0;
         }
+    }
+    if (smem_warp == 0) {
+        minb = 4;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel_hbm, 128, 0);
     }
     int32_t slots = o->max_slots > 0 ? o->max_slots : std::max(1, sms * std::max(per_sm, 1) * 4);
     // per-variable arrays in HBM only when they are not in shared memory
@@ -168,8 +175,9 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     const int64_t budget = (int64_t)((free_b + (size_t)b->ws_bytes) * 0.5);
     if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
     if (b->ws && slots == b->ws_slots && N == b->ws_N && W == b->ws_W && A == b->ws_A && C == b->ws_C &&
-        smem_warp == b->P.smem_per_warp)
+        smem_warp == b->P.smem_per_warp && minb == b->minb)
         return GPSAT_OK;
+    b->minb = minb;
     cudaFree(b->ws);
     b->ws = nullptr;
     const size_t S = slots;
@@ -486,7 +494,10 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (J) {
         const int slots = std::min<int32_t>(b->ws_slots, J);
         P.n_slots = slots;
-        cdcl::cdcl_kernel<<<(slots + 3) / 4, 128, 4 * (size_t)P.smem_per_warp, st>>>(P);
+        if (b->minb == 4)
+            cdcl::cdcl_kernel_hbm<<<(slots + 3) / 4, 128, 0, st>>>(P);
+        else
+            cdcl::cdcl_kernel_smem<<<(slots + 3) / 4, 128, 4 * (size_t)P.smem_per_warp, st>>>(P);
         P.n_slots = b->ws_slots;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_error(err, "solve kernel launch");

@@ -61,3 +61,34 @@ def cube_jobs(formulas, n_vars, depth: int, rule: str = "max_clause", scores=Non
         end += d * J
     return (np.concatenate(jf) if jf else np.zeros(0, np.int32), np.concatenate(co),
             np.concatenate(cl) if cl else np.zeros(0, np.int32))
+
+
+def autotune_depth(formulas, n_vars, depths=(4, 5, 6, 7, 8, 9, 10), sample: int = 16, options=None,
+                   rule: str = "max_clause", communities=None, log=None):
+    """Picks the split depth: solves a seeded sample of the formulas as cube
+    jobs at every candidate depth and keeps the one with the most formulas
+    decided per second (ties to the smaller depth).  Returns (depth, table)
+    with table[d] = (decided, seconds)."""
+    import time
+
+    from . import Batch
+    rng = np.random.default_rng(0)
+    pick = np.sort(rng.choice(len(formulas), size=min(sample, len(formulas)), replace=False))
+    f = [formulas[i] for i in pick]
+    nv = [int(n_vars[i]) for i in pick]
+    b = Batch(f, nv)
+    table = {}
+    best, best_rate = None, -1.0
+    for d in depths:
+        jobs = cube_jobs(f, nv, d, rule)
+        t0 = time.perf_counter()
+        out = b.solve(options, jobs=jobs)
+        dt = time.perf_counter() - t0
+        decided = int((out["verdict"] != 0).sum())
+        table[d] = (decided, dt)
+        rate = decided / dt
+        if log:
+            log(f"depth {d}: {decided}/{len(f)} decided in {dt:.2f} s")
+        if rate > best_rate:
+            best, best_rate = d, rate
+    return best, table

@@ -123,3 +123,20 @@ def test_batched_workload_sample_matches_reference(gpsat, cuda_ok, solve_golden)
     assert len(decided) >= 150
     bad = [(r["index"], r["ref_nocap"], v) for r, v in decided if r["ref_nocap"] != v]
     assert not bad, f"verdicts differ from the reference: {bad[:5]}"
+
+
+def test_split_depth_autotuner(gpsat, cuda_ok):
+    """The JobChooser depth autotuner times a sample at each candidate depth and
+    returns one of them; the cube verdicts agree with the whole-formula ones."""
+    from gpupsat_gb300 import jobs
+    ns = [400, 500, 600, 450, 550, 350]
+    formulas = [gpsat.gen_planted(500 + i, n, 4 * n, 3, 40, 0.9)[:2] for i, n in enumerate(ns)]
+    opts = gpsat.solve_options(conflict_budget=20000)
+    depth, table = jobs.autotune_depth(formulas, ns, depths=(2, 3, 4), sample=4, options=opts)
+    assert depth in (2, 3, 4) and set(table) == {2, 3, 4}
+    assert all(t[1] > 0 for t in table.values())
+    whole = gpsat.Batch(formulas, ns).solve(opts)
+    cubes = gpsat.Batch(formulas, ns).solve(opts, jobs=jobs.cube_jobs(formulas, ns, depth))
+    both = (whole["verdict"] != 0) & (cubes["verdict"] != 0)
+    assert (whole["verdict"][both] == cubes["verdict"][both]).all()
+    assert (cubes["verdict"][cubes["verdict"] != 0] == gpsat.SAT).all()    # planted: satisfiable

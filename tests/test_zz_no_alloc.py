@@ -96,3 +96,35 @@ def test_static_entry_needs_a_resident_formula(gpsat, cuda_ok):
     with pytest.raises(gpsat.GpsatError) as e:
         gpsat.bcp_run_static(f, torch.from_numpy(tl).to(dev), torch.from_numpy(to).to(dev), out, impl_cap=64)
     assert e.value.code == -9                           # GPSAT_ERR_STATE
+
+
+def test_static_entry_replays_inside_a_cuda_graph(gpsat, cuda_ok):
+    """The allocation-free entry captured once into a CUDA graph and replayed:
+    each replay re-reads the (rewritten) trail buffers and matches the
+    allocating entry point on the same trails."""
+    import torch
+    dev = torch.device("cuda:0")
+    cap = 256
+    n, T = 3000, 96
+    lits, off = gpsat.gen_random_ksat(71, n, 12600, 3)
+    f = gpsat.Formula(lits, off, n)
+    b = gpsat.BCPBatch(f, impl_cap=cap)
+    sets = [gpsat.gen_trails(72 + k, n, T, 0.02, 0.02) for k in range(3)]   # equal lengths: fixed offsets
+    assert all(np.array_equal(s[1], sets[0][1]) for s in sets)
+    d_tl = torch.from_numpy(sets[0][0]).to(dev)
+    d_to = torch.from_numpy(sets[0][1]).to(dev)
+    got = device_out(torch, T, cap, dev)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):   # the first call on the device looks its array up: before any capture
+        gpsat.bcp_run_static(f, d_tl, d_to, got, impl_cap=cap, stream=s.cuda_stream)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        gpsat.bcp_run_static(f, d_tl, d_to, got, impl_cap=cap, stream=s.cuda_stream)
+    for tl, to in sets[1:]:
+        d_tl.copy_(torch.from_numpy(tl))
+        g.replay()
+        torch.cuda.synchronize()
+        want = b.run_host(tl, to)
+        compare_bcp(to_host(got), want, label="graph replay")
+        assert np.array_equal(to_host(got)["counters"], want["counters"])
