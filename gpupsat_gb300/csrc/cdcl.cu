@@ -55,6 +55,22 @@ __device__ __forceinline__ unsigned lanemask_lt()
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
     return r;
 }
+// position of the n-th set bit of m (n >= 1, m holds at least n set bits)
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (c < n) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
 template <class T>
 __device__ __forceinline__ T wsum(T x)
 {
@@ -262,6 +278,172 @@ __device__ bool attach_watch(Ctx &C, int32_t lit, int32_t ref, int32_t blk)
 }
 
 // ---------------------------------------------------------------- BCP
+// Evaluates one watch of false literal x: keep (blocker or other watch true),
+// move (a non-false replacement at position kpos), imply l0, or conflict.
+__device__ __forceinline__ void eval_watch(const Ctx &C, int32_t x, int2 w, int &act, int32_t &blk, int32_t &imp,
+                                           int32_t &tgt, int32_t &l0, int &kpos, bool &swapped)
+{
+    int32_t *CL = C.arena + w.x + HDR;
+    const int len = (int)((uint32_t)C.arena[w.x] & LEN_MASK);
+    l0 = CL[0];
+    if (l0 == x) {
+        l0 = CL[1];
+        swapped = true;
+    }
+    const int v0 = lval(C, l0);
+    if (v0 == 1) {
+        blk = l0;
+        return;
+    }
+    // first literal at position >= 2 that is not false, four literals per
+    // 16-byte load (chunks aligned in the arena, whose slot base and capacity
+    // are multiples of 4 words)
+    int k = len;
+    int32_t lk = 0;
+    const int64_t a0 = (int64_t)w.x + HDR + 2, a1 = (int64_t)w.x + HDR + len;
+    for (int64_t c = a0 & ~int64_t(3); c < a1 && k == len; c += 4) {
+        const int4 q = *reinterpret_cast<const int4 *>(C.arena + c);
+        const int32_t qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+            const int64_t at = c + jj;
+            if (k == len && at >= a0 && at < a1 && lval(C, qq[jj]) != -1) {
+                k = (int)(at - ((int64_t)w.x + HDR));
+                lk = qq[jj];
+            }
+        }
+    }
+    blk = l0;
+    if (k < len) {
+        act = W_MOVE;
+        tgt = lk;
+        kpos = k;
+    } else {
+        act = (v0 == -1) ? W_CONFL : W_IMPLY;
+        imp = l0;
+    }
+}
+
+// Several pending literals whose watch lists fit together in one 32-wide
+// step are propagated at once: lane k takes entry k of the concatenated lists.
+// (A CDCL solver may propagate its queue in any order, and every action below
+// is valid against the state before the step, as in the one-list step.)
+// Returns the number of literals consumed (0: not applicable, the caller takes
+// the one-list path); sets confl / overflow like it.
+__device__ int propagate_multi(Ctx &C, int32_t &confl, bool &overflow)
+{
+    const int lane = C.lane;
+    const unsigned lt = lanemask_lt();
+    const int npend = min(32, C.tsize - C.qhead);
+    if (npend < 2) return 0;
+    int32_t xl = 0, sl = 0, nl = 0;
+    if (lane < npend) {
+        xl = C.trail[C.qhead + lane] ^ 1;
+        sl = C.wl_start[xl];
+        nl = C.wl_size[xl];
+    }
+    int incl = nl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    // sizes are >= 0, so the lists that fit form a prefix of the queue
+    const unsigned fit = __ballot_sync(FULL, lane < npend && incl <= 32);
+    const int K = __popc(fit);
+    if (K < 2) return 0;
+    const int total = __shfl_sync(FULL, incl, K - 1);
+    const int excl = incl - nl;
+    // entry position -> list: rank among the lists that start at or before it
+    const bool nonempty = lane < K && nl > 0;
+    const unsigned nem = __ballot_sync(FULL, nonempty);
+    const unsigned starts = __reduce_or_sync(FULL, nonempty ? (1u << excl) : 0u);
+    const bool has = lane < total;
+    int li = 0;
+    if (has) li = nth_set_bit(nem, __popc(starts & (lane == 31 ? FULL : ((2u << lane) - 1u))));
+    const int32_t x = __shfl_sync(FULL, xl, li), s = __shfl_sync(FULL, sl, li), e0 = __shfl_sync(FULL, excl, li);
+    int2 w = has ? C.watches[s + lane - e0] : make_int2(-1, 0);
+    if (__any_sync(FULL, has && (w.x < 0 || w.x >= C.arena_top || w.y < 0 || w.y >= 2 * C.n))) {
+        fail_check(C, CK_CREF);
+        confl = -1;
+        return -1;
+    }
+    // a clause in two of these lists (both its watches false): the one-list path
+    const unsigned dup = __match_any_sync(FULL, has ? w.x : -1 - lane);
+    if (__any_sync(FULL, has && (dup & lt))) return 0;
+    C.qhead += K;
+    C.props += K;
+    int act = W_KEEP;
+    int32_t blk = w.y, imp = -1, tgt = -1, l0 = 0;
+    int kpos = -1;
+    bool swapped = false;
+    if (has && lval(C, w.y) != 1) eval_watch(C, x, w, act, blk, imp, tgt, l0, kpos, swapped);
+    bool moved = false, full = false;
+    if (act == W_MOVE) {
+        moved = watch_push(C, tgt, w.x, l0);
+        full = !moved;
+    }
+    __syncwarp();
+    while (__any_sync(FULL, full)) {
+        const int ld = __ffs(__ballot_sync(FULL, full)) - 1;
+        const int32_t L = __shfl_sync(FULL, tgt, ld);
+        if (!relocate(C, L)) break;
+        if (full && tgt == L) {
+            moved = watch_push(C, tgt, w.x, l0);
+            full = !moved;
+        }
+        __syncwarp();
+    }
+    overflow |= __any_sync(FULL, full);
+    if (moved) {
+        int32_t *CL = C.arena + w.x + HDR;
+        CL[0] = l0;
+        CL[1] = tgt;
+        CL[kpos] = x;
+    }
+    const bool is_imp = act == W_IMPLY;
+    bool winner = false;
+    if (__any_sync(FULL, is_imp)) {
+        const int32_t key = is_imp ? (imp >> 1) : -1 - lane;
+        const unsigned grp = __match_any_sync(FULL, key);
+        const int lead = __ffs(grp) - 1;
+        const int32_t lead_lit = __shfl_sync(FULL, imp, lead);
+        winner = is_imp && lead == lane;
+        if (is_imp && !winner) act = (imp == lead_lit) ? W_KEEP : W_CONFL;
+    }
+    const unsigned wm = __ballot_sync(FULL, winner);
+    if (C.tsize + __popc(wm) > C.n) {
+        fail_check(C, CK_TRAIL);
+        return -1;
+    }
+    if (winner) {
+        int32_t *CL = C.arena + w.x + HDR;
+        if (swapped) {
+            CL[0] = l0;
+            CL[1] = x;
+        }
+        const int pos = C.tsize + __popc(wm & lt);
+        const int32_t v = imp >> 1;
+        C.val[v] = (imp & 1) ? 1 : -1;
+        C.level[v] = C.dlevel;
+        C.reason[v] = w.x;
+        C.trail[pos] = imp;
+    }
+    C.tsize += __popc(wm);
+    const unsigned cm = __ballot_sync(FULL, act == W_CONFL);
+    if (cm) confl = __shfl_sync(FULL, w.x, __ffs(cm) - 1);
+    // each list keeps its entries that did not move, in order, at its start
+    const bool kept = has && !moved;
+    const unsigned km = __ballot_sync(FULL, kept);
+    const unsigned seg = __match_any_sync(FULL, has ? li : -1 - lane);
+    if (kept) C.watches[s + __popc(km & lt & seg)] = make_int2(w.x, blk);
+    __syncwarp();
+    // new list sizes: the first lane of each list writes its count
+    if (has && (seg & lt) == 0) C.wl_size[x] = __popc(km & seg);
+    __syncwarp();
+    return K;
+}
+
 // Returns the conflicting clause reference, or -1.
 __device__ int32_t propagate(Ctx &C)
 {
@@ -270,6 +452,23 @@ __device__ int32_t propagate(Ctx &C)
     int32_t confl = -1;
     int guard = 0;
     while (C.qhead < C.tsize && confl < 0) {
+        bool moverflow = false;
+        const int took = propagate_multi(C, confl, moverflow);
+        if (took < 0) return -1;
+        if (took > 0) {
+            if (moverflow) {
+                if (!rebuild_watches(C)) {
+                    out_of(C, RS_WATCHES);
+                    return -1;
+                }
+                if (confl < 0) C.qhead = (C.dlevel > 0) ? C.tlim[C.dlevel - 1] : 0;
+                if (++guard > 64) {
+                    out_of(C, RS_REBUILD_LOOP);
+                    return -1;
+                }
+            }
+            continue;
+        }
         const int32_t p = C.trail[C.qhead];
         C.qhead++;
         C.props++;
