@@ -358,7 +358,7 @@ __device__ int propagate_multi(Ctx &C, int32_t &confl, bool &overflow)
     const bool nonempty = lane < K && nl > 0;
     const unsigned nem = __ballot_sync(FULL, nonempty);
     const unsigned starts = __reduce_or_sync(FULL, nonempty ? (1u << excl) : 0u);
-    const bool has = lane < total;
+    bool has = lane < total;
     int li = 0;
     if (has) li = nth_set_bit(nem, __popc(starts & (lane == 31 ? FULL : ((2u << lane) - 1u))));
     const int32_t x = __shfl_sync(FULL, xl, li), s = __shfl_sync(FULL, sl, li), e0 = __shfl_sync(FULL, excl, li);
@@ -368,11 +368,19 @@ __device__ int propagate_multi(Ctx &C, int32_t &confl, bool &overflow)
         confl = -1;
         return -1;
     }
-    // a clause in two of these lists (both its watches false): the one-list path
+    // a clause in two of these lists (both its watches false): take only the
+    // lists before the later one (the one-list path when that leaves one)
     const unsigned dup = __match_any_sync(FULL, has ? w.x : -1 - lane);
-    if (__any_sync(FULL, has && (dup & lt))) return 0;
-    C.qhead += K;
-    C.props += K;
+    const int kd = __reduce_min_sync(FULL, (has && (dup & lt)) ? (unsigned)li : 32u);
+    int K2 = K;
+    if (kd < K2) {
+        K2 = kd;
+        if (K2 < 2) return 0;
+        has = lane < __shfl_sync(FULL, incl, K2 - 1);
+        if (!has) w = make_int2(-1, 0);
+    }
+    C.qhead += K2;
+    C.props += K2;
     int act = W_KEEP;
     int32_t blk = w.y, imp = -1, tgt = -1, l0 = 0;
     int kpos = -1;
@@ -441,7 +449,7 @@ __device__ int propagate_multi(Ctx &C, int32_t &confl, bool &overflow)
     // new list sizes: the first lane of each list writes its count
     if (has && (seg & lt) == 0) C.wl_size[x] = __popc(km & seg);
     __syncwarp();
-    return K;
+    return K2;
 }
 
 // Returns the conflicting clause reference, or -1.
