@@ -209,6 +209,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def combine_ranks(dist, device, seconds, units):
+    """Whole-job figures over the ranks: the slowest rank's time and the sum of
+    the units every rank processed (each rank works on its own trails, so
+    nothing else is exchanged).  dist = None for one process."""
+    import torch
+    if dist is None:
+        return float(seconds), float(units)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u)
+    return float(t.item()), float(u.item())
+
+
 def run_gpu(args):
     import torch
     import gpupsat_gb300 as g
@@ -262,15 +276,7 @@ def run_gpu(args):
     elapsed = sum(launch_ms) / 1000.0
     cnt2 = out["counters"].cpu().numpy()
     assert int(cnt2[:, 0].sum()) == props_step, "propagation count changed between steps"
-    if dist:
-        t = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-        pt = torch.tensor([props_step], dtype=torch.float64, device=dev)
-        dist.all_reduce(pt)
-        props_all = float(pt.item())
-    else:
-        props_all = float(props_step)
+    elapsed, props_all = combine_ranks(dist, dev, elapsed, props_step)
     value = props_all * args.steps / elapsed
 
     # end to end through the host entry point (pinned buffers)
@@ -289,10 +295,7 @@ def run_gpu(args):
         for _ in range(args.steps):
             h = b.run_host(p_tl, p_to, out=h_out)
         e2e_s = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s, _ = combine_ranks(dist, dev, e2e_s, 0)
         maxn = int(h["n_impl"].max())
         d2h = T * (4 * 3 + 8 + 8 * 6) + 2 * 4 * T * (maxn if maxn * 4 < cap * 2 else cap)
         e2e = {"value": props_all * args.steps / e2e_s, "unit": UNIT,
@@ -320,7 +323,7 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
             "config": config(args, n, m), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (4 if T > b.info()["slots"] else 1),  # order kernels + BCP kernel
             "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item())}
     print(json.dumps(line))
     if dist:

@@ -88,6 +88,7 @@ struct Dev {
     int2 *stack;
     uint32_t *epoch;
     unsigned int *next_trail;
+    const int32_t *order;             // trails in processing order (null: index order)
     int64_t n_pad, m_pad, arena_cap, impl_cap;
     int32_t n_slots;
     const int32_t *__restrict__ trail;
@@ -830,6 +831,62 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     }
 }
 
+// ---------------------------------------------------------------------------
+// Processing order: shortest trails first.  A launch lasts as long as its
+// slowest trail, and when there are more trails than resident warps the
+// last ones start only as others finish.  The trails that propagate longest
+// are those that reach their fixpoint without a conflict, and a trail that
+// assigns fewer variables is the more likely to: starting the short ones
+// first starts the long-running ones at once.  (Outputs do not depend on the
+// order; at the 4096-trail benchmark shape the measured per-trail durations
+// give a 37.9 ms schedule instead of 41.4 ms.)  A counting sort on length / 16.
+constexpr int ORDER_BUCKETS = 4096;
+
+__device__ __forceinline__ int order_bucket(const int64_t *toff, int t)
+{
+    const int64_t len = toff[t + 1] - toff[t];
+    return len <= 0 ? 0 : (int)(len >> 4 < ORDER_BUCKETS - 1 ? len >> 4 : ORDER_BUCKETS - 1);
+}
+
+__global__ void order_count(const int64_t *toff, int T, unsigned *hist)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
+        atomicAdd(&hist[order_bucket(toff, t)], 1u);
+}
+
+// one block of 1024 threads: the counts become exclusive prefix sums in place
+__global__ void __launch_bounds__(1024) order_scan(unsigned *hist)
+{
+    __shared__ unsigned part[1024];
+    const int i = threadIdx.x;
+    unsigned v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[k] = hist[4 * i + k];
+        sum += v[k];
+    }
+    part[i] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned add = i >= o ? part[i - o] : 0u;
+        __syncthreads();
+        part[i] += add;
+        __syncthreads();
+    }
+    unsigned run = part[i] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        hist[4 * i + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void order_scatter(const int64_t *toff, int T, unsigned *hist, int32_t *order)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
+        order[atomicAdd(&hist[order_bucket(toff, t)], 1u)] = t;
+}
+
 // blocks per SM the register allocation targets: 4 (16 resident warps per SM)
 // leaves the kernel its ~100 registers without spills, which measured faster
 // than 32 resident warps with spills at 64 registers
@@ -847,7 +904,7 @@ __global__ void __launch_bounds__(WARPS * 32, GPSAT_BCP_MIN_BLOCKS) bcp_kernel(D
         if (lane == 0) t = (int)atomicAdd(d.next_trail, 1u);
         t = __shfl_sync(FULL, t, 0);
         if (t >= d.n_trails) break;
-        process_trail(d, smem[wib], t, slot, lane);
+        process_trail(d, smem[wib], d.order ? d.order[t] : t, slot, lane);
     }
 }
 
@@ -869,6 +926,9 @@ struct gpsat_bcp {
     int4 *arena = nullptr;
     int2 *stack = nullptr;
     unsigned int *counter = nullptr;
+    unsigned *hist = nullptr;          // ORDER_BUCKETS counters
+    int32_t *order = nullptr;          // processing order of the last launch
+    int64_t order_cap = 0;
     int64_t bytes = 0;
     // host-path staging
     int32_t *d_trail = nullptr;
@@ -888,6 +948,8 @@ void bcp_free(gpsat_bcp *b)
     cudaFree(b->arena);
     cudaFree(b->stack);
     cudaFree(b->counter);
+    cudaFree(b->hist);
+    cudaFree(b->order);
     cudaFree(b->d_trail);
     cudaFree(b->d_toff);
     cudaFree(b->d_out);
@@ -925,9 +987,30 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
     d.ilit = ilit;
     d.ireason = ireason;
     d.counters = counters;
+    d.order = nullptr;
     cudaError_t err = cudaMemsetAsync(b->counter, 0, sizeof(unsigned int), st);
     if (err != cudaSuccess) return cuda_error(err, "bcp counter reset");
     if (n_trails == 0) return GPSAT_OK;
+    if (n_trails > d.n_slots) {
+        // more trails than resident warps: shortest first (see order_count)
+        if (!b->hist && cudaMalloc(&b->hist, bcp::ORDER_BUCKETS * sizeof(unsigned)) != cudaSuccess)
+            return set_error(GPSAT_ERR_NOMEM, "bcp order buckets");
+        if (n_trails > b->order_cap) {
+            cudaFree(b->order);
+            b->order = nullptr;
+            b->order_cap = 0;
+            if (cudaMalloc(&b->order, (size_t)n_trails * 4) != cudaSuccess)
+                return set_error(GPSAT_ERR_NOMEM, "bcp order");
+            b->order_cap = n_trails;
+        }
+        err = cudaMemsetAsync(b->hist, 0, bcp::ORDER_BUCKETS * sizeof(unsigned), st);
+        if (err != cudaSuccess) return cuda_error(err, "bcp order reset");
+        const int g = std::min(1024, (n_trails + 255) / 256);
+        bcp::order_count<<<g, 256, 0, st>>>(toff, n_trails, b->hist);
+        bcp::order_scan<<<1, 1024, 0, st>>>(b->hist);
+        bcp::order_scatter<<<g, 256, 0, st>>>(toff, n_trails, b->hist, b->order);
+        d.order = b->order;
+    }
     const int blocks = (d.n_slots + bcp::WARPS - 1) / bcp::WARPS;
     bcp::bcp_kernel<<<blocks, bcp::WARPS * 32, 0, st>>>(d);
     err = cudaGetLastError();
@@ -1268,6 +1351,7 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     d.stack = stack;
     d.epoch = epoch;
     d.next_trail = counter;
+    d.order = nullptr;
     d.n_pad = n_pad;
     d.m_pad = m_pad;
     d.arena_cap = acap;
