@@ -369,15 +369,20 @@ class Batch:
         p = None if phase is None else np.ascontiguousarray(phase, np.int8)
         check(lib().gpsat_batch_set_seeds(self._h, _p(a), _p(p)))
 
-    def solve(self, options: SolveOptions | None = None, jobs=None, participation: bool = False) -> dict:
-        """jobs: None, or (job_formula int32[J], cube_offsets int64[J+1], cube_lits int32[...])."""
+    def solve(self, options: SolveOptions | None = None, jobs=None, participation: bool | int = False) -> dict:
+        """jobs: None, or (job_formula int32[J], cube_offsets int64[J+1], cube_lits int32[...]).
+        participation: True / 1 logs per-variable conflict participation
+        (out["participation"]); 2 also learnt-clause occurrences
+        (out["learnt_occurrences"])."""
         F = self.n_formulas
+        V = int(self.var_off[-1])
         o = options or solve_options()
-        if participation:
-            o.log_participation = 1
-        out = dict(verdict=np.zeros(F, np.int32), model=np.zeros(int(self.var_off[-1]), np.int8),
+        level = int(participation)
+        if level:
+            o.log_participation = level
+        out = dict(verdict=np.zeros(F, np.int32), model=np.zeros(V, np.int8),
                    stats=np.zeros((F, 9), np.int64), model_ok=np.zeros(F, np.int32),
-                   participation=np.zeros(int(self.var_off[-1]), np.int32) if participation else None)
+                   participation=np.zeros(V * (2 if level >= 2 else 1), np.int32) if level else None)
         jf = co = cl = None
         nj = 0
         if jobs is not None:
@@ -388,6 +393,9 @@ class Batch:
         check(lib().gpsat_batch_solve(self._h, ctypes.byref(o), _p(jf), _p(co), _p(cl), nj, _p(out["verdict"]),
                                       _p(out["model"]), _p(out["stats"]), _p(out["model_ok"]),
                                       _p(out["participation"])))
+        if level >= 2:
+            out["learnt_occurrences"] = out["participation"][V:]
+            out["participation"] = out["participation"][:V]
         return out
 
     def model_of(self, out: dict, f: int) -> np.ndarray:

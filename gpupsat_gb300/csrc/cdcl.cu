@@ -109,6 +109,7 @@ struct Ctx {
     int32_t *arena, *crefs;
     int32_t *sm64;   // 64 ints of shared memory for this warp
     int32_t *part;
+    int32_t *occ;    // per variable: occurrences in learnt clauses (optional)
     int64_t WCAP, ACAP, CCAP;
     int64_t wtop;    // first watch entry of the free tail (lists outgrown are moved there)
     // warp-uniform state
@@ -696,7 +697,7 @@ __device__ void analyze(Ctx &C, int32_t confl, int &out_len, int &bt_level, int 
             if (take) {
                 C.seen[v] = 1;
                 bump(C, v, big);
-                if (C.part) C.part[v]++;
+                if (C.part) atomicAdd(&C.part[v], 1);
                 cur = C.level[v] >= C.dlevel;
             }
             pathC += __popc(__ballot_sync(FULL, cur));
@@ -1090,6 +1091,7 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
     C.why = 0;
     C.conflicts = C.decisions = C.props = C.restarts = C.reduces = C.rebuilds = 0;
     C.part = (P.part && o.log_participation) ? P.part + voff : nullptr;
+    C.occ = (P.part && o.log_participation >= 2) ? P.part + P.var_total + voff : nullptr;
     for (int v = lane; v < C.n; v += 32) {
         C.val[v] = 0;
         C.seen[v] = 0;
@@ -1177,6 +1179,8 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
                 result = R_UNKNOWN;
                 break;
             }
+            if (C.occ)
+                for (int k = lane; k < len; k += 32) atomicAdd(&C.occ[C.learnt[k] >> 1], 1);
             backtrack(C, bt);
             int32_t r = -1;
             if (len >= 2) {

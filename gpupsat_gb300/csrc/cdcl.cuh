@@ -34,7 +34,7 @@ struct Opts {
     int32_t minimize = 1;
     int64_t conflict_budget = 100000;
     int32_t phase_init = 0;          // 0: negative first, 1: positive first
-    int32_t log_participation = 0;
+    int32_t log_participation = 0;   // 1: participation counts; 2: and learnt-clause occurrences
     int32_t check_every = 256;       // conflicts between cancellation checks
 };
 
@@ -66,7 +66,9 @@ struct Params {
     int32_t *job_verdict;
     int64_t *job_stats;          // NSTATS per job
     int8_t *model;               // per (instance, var): +1 / -1
-    int32_t *part;               // per (instance, var): conflict participation (optional)
+    int32_t *part;               // per (instance, var): conflict participation (optional); with
+                                 // log_participation 2 followed by learnt-clause occurrences
+    int64_t var_total;           // variables of all instances (the second half's offset)
     // workspace
     int32_t n_slots;
     int32_t N;                   // max vars (padded to 16)

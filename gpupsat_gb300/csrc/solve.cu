@@ -89,6 +89,7 @@ struct gpsat_batch {
     // per-formula device outputs
     int8_t *d_model = nullptr;
     int32_t *d_state = nullptr, *d_verdict = nullptr, *d_ok = nullptr, *d_part = nullptr;
+    int64_t part_cap = 0;
     float *d_seed_act = nullptr;
     int8_t *d_seed_phase = nullptr;
     // jobs
@@ -443,7 +444,16 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         b->cube_cap = (int64_t)cubes.size();
     }
     const int64_t V = b->var_off[F];
-    if (o.log_participation && !b->d_part && !dalloc(&b->d_part, V)) return set_error(GPSAT_ERR_NOMEM, "part");
+    if (o.log_participation < 0 || o.log_participation > 2)
+        return set_error(GPSAT_ERR_ARG, "log_participation must be 0, 1 or 2");
+    const int64_t PV = o.log_participation >= 2 ? 2 * V : V;
+    if (o.log_participation && b->part_cap < PV) {
+        cudaFree(b->d_part);
+        b->d_part = nullptr;
+        b->part_cap = 0;
+        if (!dalloc(&b->d_part, PV)) return set_error(GPSAT_ERR_NOMEM, "part");
+        b->part_cap = PV;
+    }
     cudaStream_t st = 0;
     bool ok = true;
     if (J) {
@@ -457,7 +467,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     ok = ok && cudaMemsetAsync(b->d_state, 0, F * 4, st) == cudaSuccess &&
          cudaMemsetAsync(b->d_model, 0, V, st) == cudaSuccess &&
          cudaMemsetAsync(b->d_counter, 0, 4, st) == cudaSuccess;
-    if (ok && o.log_participation) ok = cudaMemsetAsync(b->d_part, 0, V * 4, st) == cudaSuccess;
+    if (ok && o.log_participation) ok = cudaMemsetAsync(b->d_part, 0, PV * 4, st) == cudaSuccess;
     if (!ok) return cuda_error(cudaGetLastError(), "solve setup");
     cdcl::Params &P = b->P;
     P.o.decide = o.decide;
@@ -491,6 +501,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     P.job_stats = b->d_job_stats;
     P.model = b->d_model;
     P.part = o.log_participation ? b->d_part : nullptr;
+    P.var_total = V;
     if (J) {
         const int slots = std::min<int32_t>(b->ws_slots, J);
         P.n_slots = slots;
@@ -567,7 +578,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (model_ok && cudaMemcpyAsync(model_ok, b->d_ok, F * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return cuda_error(cudaGetLastError(), "check copy");
     if (participation && o.log_participation &&
-        cudaMemcpyAsync(participation, b->d_part, V * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        cudaMemcpyAsync(participation, b->d_part, PV * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return cuda_error(cudaGetLastError(), "participation copy");
     err = cudaStreamSynchronize(st);
     if (err != cudaSuccess) return cuda_error(err, "model check");

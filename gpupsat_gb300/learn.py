@@ -12,8 +12,9 @@ inputs.
 Every forward and backward step runs in libgpsat's hand-written kernels
 (gnn.cu: tcgen05 matrix products, message sums, heads, Adam); torch only
 allocates device memory.  The training labels come from the solver itself:
-per-variable conflict participation logged during budgeted solves
-(Batch.solve(participation=True)) and the models of satisfiable instances.
+per-variable conflict participation and learnt-clause occurrence counts
+logged during budgeted solves (Batch.solve(participation=2)) and the models
+of satisfiable instances.
 
 Variable features F_v (64 wide, zero padded): log(1 + occurrences) by
 polarity, log(1 + number of clauses of length k holding v) for k = 3..7
@@ -273,23 +274,26 @@ class Pass:
 
 # ---------------------------------------------------------------- labels and seeds
 def participation_targets(formulas, n_vars, conflict_budget=20000, options=None):
-    """Solves every formula once with conflict-participation logging.
-    Returns per-variable arrays (all formulas concatenated): activity target
-    y = log1p(part) / log1p(max part of its formula), phase target (1 where the
-    model sets the variable true; SAT formulas only), and the solve output."""
+    """Solves every formula once, logging per-variable conflict participation
+    and learnt-clause occurrences.  Returns per-variable arrays (all formulas
+    concatenated): activity target y = mean of log1p(count) / log1p(max count
+    of its formula) over the two counts, phase target (1 where the model sets
+    the variable true; SAT formulas only), and the solve output."""
     from . import Batch, solve_options
     b = Batch(formulas, n_vars)
     o = options or solve_options(conflict_budget=conflict_budget)
-    out = b.solve(o, participation=True)
-    part = out["participation"].astype(np.float64)
+    out = b.solve(o, participation=2)
+    counts = (out["participation"].astype(np.float64), out["learnt_occurrences"].astype(np.float64))
+    part = counts[0]
     y = np.zeros(len(part), np.float32)
     t = np.zeros(len(part), np.float32)
     has_phase = np.zeros(len(part), bool)
     for f in range(b.n_formulas):
         a, e = b.var_off[f], b.var_off[f + 1]
-        mx = part[a:e].max() if e > a else 0
-        if mx > 0:
-            y[a:e] = np.log1p(part[a:e]) / np.log1p(mx)
+        for c in counts:
+            mx = c[a:e].max() if e > a else 0
+            if mx > 0:
+                y[a:e] += 0.5 * (np.log1p(c[a:e]) / np.log1p(mx)).astype(np.float32)
         if out["verdict"][f] == 10:
             t[a:e] = (out["model"][a:e] > 0)
             has_phase[a:e] = True

@@ -183,7 +183,8 @@ typedef struct {
     int64_t conflict_budget;   /* per job; reaching it ends the job UNKNOWN (0 = none) */
     int32_t phase_init;        /* first polarity of an unseeded variable: 0 false, 1 true */
     int32_t max_slots;         /* jobs in flight (0 = as many as the GPU keeps resident) */
-    int32_t log_participation; /* count, per variable, the conflicts whose analysis saw it */
+    int32_t log_participation; /* 1: count, per variable, the conflicts whose analysis saw it;
+                                  2: also its occurrences in learnt clauses */
     int32_t reserved[5];
 } gpsat_solve_options;
 
@@ -215,7 +216,9 @@ int gpsat_batch_set_seeds(gpsat_batch *b, const float *activity, const int8_t *p
  * +1 true / -1 false, concatenated; may be NULL), stats (GPSAT_SOLVE_NSTATS
  * each; may be NULL), model_ok (device checker: 1 every original clause holds
  * a true literal, 0 not, -1 no model; may be NULL), participation (int32 per
- * variable, with log_participation; may be NULL). */
+ * variable, with log_participation; with log_participation 2 the array holds
+ * twice the variables: participation, then learnt-clause occurrences; may be
+ * NULL). */
 int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt, const int32_t *job_formula,
                       const int64_t *cube_offsets, const int32_t *cube_lits, int32_t n_jobs, int32_t *verdicts,
                       int8_t *models, int64_t *stats, int32_t *model_ok, int32_t *participation);
