@@ -90,6 +90,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_gen_random_ksat": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]),
         "gpsat_gen_trails": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                             ctypes.c_double, _vp, _vp]),
+        "gpsat_dimacs_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64, _c_i32p, _c_i64p, _c_i64p, _c_i32p,
+                                              _c_i64p, _vp, _vp]),
         "gpsat_gen_planted": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_double, _vp, _vp]),
         # learned seeding kernels (device pointers)
@@ -149,6 +151,22 @@ def gen_random_ksat(seed: int, n_vars: int, n_clauses: int, k: int = 3) -> tuple
     lits = np.empty(n_clauses * k, dtype=np.int32)
     check(lib().gpsat_gen_random_ksat(seed, n_vars, n_clauses, k, _p(lits)))
     return lits, np.arange(0, n_clauses * k + 1, k, dtype=np.int64)
+
+
+def parse_dimacs(text: str | bytes) -> dict:
+    """DIMACS CNF text -> dict(lits, offsets, n_vars, header_vars, header_clauses)
+    (gpsat_dimacs_parse; n_vars is the highest variable found, as the
+    reference's reader sets it)."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    nv, nc, nl, hv, hc = (ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int64())
+    L = lib()
+    check(L.gpsat_dimacs_parse(data, len(data), ctypes.byref(nv), ctypes.byref(nc), ctypes.byref(nl),
+                               ctypes.byref(hv), ctypes.byref(hc), None, None))
+    lits = np.empty(nl.value, np.int32)
+    off = np.empty(nc.value + 1, np.int64)
+    check(L.gpsat_dimacs_parse(data, len(data), ctypes.byref(nv), ctypes.byref(nc), ctypes.byref(nl),
+                               ctypes.byref(hv), ctypes.byref(hc), _p(lits), _p(off)))
+    return dict(lits=lits, offsets=off, n_vars=nv.value, header_vars=hv.value, header_clauses=hc.value)
 
 
 def gen_planted(seed: int, n_vars: int, n_clauses: int, k: int = 3, communities: int = 40, p_in: float = 0.9):

@@ -107,7 +107,8 @@ extern "C" int gpsat_dimacs_parse(const char *text, int64_t len, int32_t *n_vars
         if (!read_int(c, x))
             return set_error(GPSAT_ERR_PARSE, "line " + std::to_string(c.line) + ": expected an integer literal");
         if (x == 0) {
-            if (cur == 0) return set_error(GPSAT_ERR_PARSE, "line " + std::to_string(c.line) + ": empty clause");
+            // "0" alone is an empty clause, as the reference's grammar reads it
+            // (the formula is then unsatisfiable)
             if (offsets) offsets[nc + 1] = nl;
             nc++;
             cur = 0;

@@ -172,12 +172,17 @@ int prepare_formula(const int32_t *lits, const int64_t *offsets, int32_t n_vars,
     if (n_clauses >= INT32_MAX / 2) return set_error(GPSAT_ERR_CAPACITY, "too many clauses (limit 2^30)");
     if (offsets && offsets[0] != 0) return set_error(GPSAT_ERR_FORMULA, "offsets[0] must be 0");
     Cnf f;
-    f.cls.resize(n_clauses);
+    f.cls.reserve(n_clauses);
+    bool has_empty = false;  // an empty clause: the formula is unsatisfiable
     for (int64_t c = 0; c < n_clauses; c++) {
         int64_t b = offsets[c], e = offsets[c + 1];
         if (e < b) return set_error(GPSAT_ERR_FORMULA, "offsets must be non-decreasing");
-        if (e == b) return set_error(GPSAT_ERR_FORMULA, "empty clause at index " + std::to_string(c));
-        auto &cl = f.cls[c];
+        if (e == b) {
+            has_empty = true;
+            continue;
+        }
+        f.cls.emplace_back();
+        auto &cl = f.cls.back();
         cl.resize(e - b);
         for (int64_t i = b; i < e; i++) {
             int32_t d = lits[i];
@@ -190,7 +195,8 @@ int prepare_formula(const int32_t *lits, const int64_t *offsets, int32_t n_vars,
     out = HostFormula();
     out.n_vars = n_vars;
     remove_repeated(f, n_vars);
-    if (f.cls.empty()) out.verdict = GPSAT_SAT;
+    if (has_empty) out.verdict = GPSAT_UNSAT;
+    else if (f.cls.empty()) out.verdict = GPSAT_SAT;
     if (out.verdict == GPSAT_UNKNOWN) {
         UnitRemover ur(f, n_vars);
         ur.process();

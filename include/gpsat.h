@@ -30,7 +30,7 @@ extern "C" {
 #define GPSAT_ERR_ARG (-1)       /* bad argument (null pointer, negative size ...) */
 #define GPSAT_ERR_CUDA (-2)      /* a CUDA call failed; gpsat_last_error() has the text */
 #define GPSAT_ERR_NOMEM (-3)     /* host or device allocation failed */
-#define GPSAT_ERR_FORMULA (-4)   /* literal out of range, empty clause, ... */
+#define GPSAT_ERR_FORMULA (-4)   /* literal out of range, bad offsets, ... */
 #define GPSAT_ERR_PARSE (-5)     /* malformed DIMACS text */
 #define GPSAT_ERR_CAPACITY (-6)  /* a size exceeds a documented limit */
 #define GPSAT_ERR_NODEVICE (-7)  /* no CUDA device visible */
@@ -84,7 +84,8 @@ int gpsat_formula_create(const int32_t *lits, const int64_t *offsets, int32_t n_
                          int64_t n_clauses, gpsat_formula **out);
 int gpsat_formula_destroy(gpsat_formula *f);
 /* Sizes after preprocessing and the preprocessing verdict (GPSAT_UNKNOWN,
- * GPSAT_SAT when every clause was removed, GPSAT_UNSAT on a unit conflict). */
+ * GPSAT_SAT when every clause was removed, GPSAT_UNSAT on a unit conflict or
+ * an empty clause). */
 int gpsat_formula_info(const gpsat_formula *f, int32_t *n_vars, int64_t *n_clauses,
                        int64_t *n_lits, int32_t *preproc_verdict, int64_t *n_solved);
 /* Copies out the preprocessed clauses (DIMACS, CSR), the literals fixed by

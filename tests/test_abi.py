@@ -39,8 +39,11 @@ def test_formula_validation(gpsat):
         gpsat.Formula(np.array([1, 5], np.int32), np.array([0, 2], np.int64), 3)
     assert e.value.code == -4
     with pytest.raises(gpsat.GpsatError) as e:
-        gpsat.Formula(np.array([1, 2], np.int32), np.array([0, 0, 2], np.int64), 3)  # empty clause
+        gpsat.Formula(np.array([1, 2], np.int32), np.array([0, 2, 1], np.int64), 3)  # offsets going back
     assert e.value.code == -4
+    # an empty clause is not an error: the formula is unsatisfiable
+    f = gpsat.Formula(np.array([1, 2], np.int32), np.array([0, 0, 2], np.int64), 3)
+    assert f.info()["verdict"] == gpsat.UNSAT
 
 
 def test_preprocessing_decides_trivial_formulas(gpsat):
@@ -115,3 +118,24 @@ def test_cube_jobs_follow_the_reference_chooser(gpsat):
     assert cl.reshape(4, 2).tolist() == [[3, 2], [3, -2], [-3, 2], [-3, -2]]
     jf, co, cl = jobs.cube_jobs([(lits, None), (lits, None)], [3, 3], depth=0)
     assert list(jf) == [0, 1] and list(co) == [0, 0, 0] and len(cl) == 0
+
+
+def test_dimacs_parser(gpsat):
+    # the reference's grammar (FileManager/CnfReader.cpp:40-47): comments, then
+    # the header, then clauses terminated by 0; the highest variable found wins
+    text = "c a comment\nc\n\np cnf 3 2\n1 -2 0\n2 3 -1 0\n"
+    d = gpsat.parse_dimacs(text)
+    assert d["n_vars"] == 3 and d["header_vars"] == 3 and d["header_clauses"] == 2
+    assert list(d["lits"]) == [1, -2, 2, 3, -1] and list(d["offsets"]) == [0, 2, 5]
+    # the header may undercount; several clauses on a line and a trailing % are accepted
+    d = gpsat.parse_dimacs("p cnf 2 1\n1 4 0 -4 2 0\n%\n0\n")
+    assert d["n_vars"] == 4 and list(d["offsets"]) == [0, 2, 4]
+    # "0" alone is an empty clause: the formula is unsatisfiable
+    d = gpsat.parse_dimacs("p cnf 2 2\n1 2 0\n0\n")
+    assert list(d["offsets"]) == [0, 2, 2]
+    f = gpsat.Formula(d["lits"], d["offsets"], 2)
+    assert f.info()["verdict"] == gpsat.UNSAT
+    for bad in ("1 2 0\n", "p cnf x 1\n1 0\n", "p cnf 2 1\n1 2\n", "p dnf 2 1\n1 0\n", "p cnf 2 1\n1 a 0\n"):
+        with pytest.raises(gpsat.GpsatError) as e:
+            gpsat.parse_dimacs(bad)
+        assert e.value.code == -5, bad
