@@ -48,7 +48,7 @@ UNIT = "props/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpsat", choices=["gpsat", "reference"])
     ap.add_argument("--n-vars", type=int, default=1_000_000)
