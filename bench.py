@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-trails", type=int, default=4096)
+    ap.add_argument("--slots", type=int, default=None,
+                    help="bcp: trails in flight (default: the fastest of 1, 3/4, 1/2, 3/8 of the resident "
+                         "warps, timed on warm-up launches)")
     ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding"],
                     help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
                          "planted: planted community instances split into JobChooser cubes; "
@@ -255,6 +258,15 @@ def run_gpu(args):
     for _ in range(args.warmup):
         b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
     stream.synchronize()
+    # trails in flight: a launch lasts as long as its longest trails, which
+    # wait on memory the other trails load too, so fewer slots can finish
+    # sooner; chosen on untimed launches (outputs do not depend on it)
+    if args.slots is None:
+        tuning = b.tune_slots(d_tl, d_to, out, stream.cuda_stream)
+    else:
+        b.set_active_slots(args.slots)
+        tuning = None
+    active = b.active or b.info()["slots"]
     cnt = out["counters"].cpu().numpy()
     props_step = int(cnt[:, 0].sum())
     bytes_step = alg_bytes(cnt)
@@ -322,8 +334,10 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
-            "config": config(args, n, m), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps * (4 if T > b.info()["slots"] else 1),  # order kernels + BCP kernel
+            "config": {**config(args, n, m), "slots": active,
+                       "slot_tuning_ms": {str(k): round(v, 3) for k, v in tuning.items()} if tuning else None},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": args.steps * (4 if T > active else 1),  # order kernels + BCP kernel
             "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item())}
     print(json.dumps(line))
     if dist:

@@ -387,16 +387,24 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             ndyn = __shfl_sync(FULL, ndyn, 0);
             dyn_done = __shfl_sync(FULL, dyn_done, 0);
         }
+        // Window position p is evaluated by lane p.  Entries from the initial
+        // lists are loaded straight into that lane's registers (g*: the
+        // current scan, h*: the look-ahead scans), so the loads of both kinds
+        // are in flight together and nothing waits on them before the
+        // evaluation; only the added-list entries go through shared memory.
         int nent = ndyn;
         int take0 = 0;
+        int4 g0 = make_int4(0, 0, 0, 0), g1 = g0, h0 = g0, h1 = g0;
         if (dyn_done) {
             take0 = min(32 - nent, (int)(cur_wend - cur_wk));
-            if (lane < take0) {
-                sm.e0[nent + lane] = d.w0ent[2 * (size_t)(cur_wk + lane)];
-                sm.e1[nent + lane] = d.w0ent[2 * (size_t)(cur_wk + lane) + 1];
+            if (lane >= nent && lane < nent + take0) {
+                const size_t w = cur_wk + (uint32_t)(lane - nent);
+                g0 = d.w0ent[2 * w];
+                g1 = d.w0ent[2 * w + 1];
             }
             nent += take0;
         }
+        const int nent0 = nent;
         if (lane == 0) {
             sm.sc_var[0] = cur_var;
             sm.sc_begin[0] = 0;
@@ -472,8 +480,8 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 const uint32_t aj = __shfl_sync(FULL, a, jj < 0 ? 0 : jj);
                 if (lane >= nent && lane < total) {
                     const size_t w = aj + (uint32_t)(lane - nent - ej);
-                    sm.e0[lane] = d.w0ent[2 * w];
-                    sm.e1[lane] = d.w0ent[2 * w + 1];
+                    h0 = d.w0ent[2 * w];
+                    h1 = d.w0ent[2 * w + 1];
                 }
                 nent = total;
                 nsc = 1 + K;
@@ -483,8 +491,8 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
 
         // ---- evaluate every entry of the window at once
         const bool has = lane < nent;
-        const int4 en = has ? sm.e0[lane] : make_int4(0, 0, 0, 0);
-        const int4 el = has ? sm.e1[lane] : make_int4(0, 0, 0, 0);
+        const int4 en = lane < ndyn ? sm.e0[lane] : (lane < nent0 ? g0 : h0);
+        const int4 el = lane < ndyn ? sm.e1[lane] : (lane < nent0 ? g1 : h1);
         const int32_t sv = sm.sc_var[my_scan];
         // lane s (1 <= s < nsc) checks whether window scan s starts with added clauses
         const int32_t scan_v = (lane >= 1 && lane < nsc) ? sm.sc_var[lane] : -1;
@@ -639,13 +647,15 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             // a later window scan whose list starts with added clauses
             if (scan_v >= 0 && (scan_h >> 24) == e) key = min(key, key_before(scan_b, lane));
             // a move of this lane that lands in a later window scan's list
-            if (valid && (r.act == A_SW1 || r.act == A_SW2)) {
-                for (int s = my_scan + 1; s < nsc; s++) {
-                    const int32_t vs = sm.sc_var[s];
-                    if (vs == r.t1 || vs == r.t2) {
-                        key = min(key, key_before(sm.sc_begin[s], s));
-                        break;
-                    }
+            // (lane s holds window scan s's variable and start; the loop is
+            // uniform, so its shuffles are independent and overlap, and the
+            // smallest key is the first such scan)
+            const bool mv = valid && (r.act == A_SW1 || r.act == A_SW2);
+            if (nsc > 1 && __any_sync(FULL, mv)) {
+                for (int s = 1; s < nsc; s++) {
+                    const int32_t vs = __shfl_sync(FULL, scan_v, s);
+                    const int bs = __shfl_sync(FULL, scan_b, s);
+                    if (mv && s > my_scan && (vs == r.t1 || vs == r.t2)) key = min(key, key_before(bs, s));
                 }
             }
         }
@@ -920,6 +930,7 @@ struct gpsat_bcp {
     const gpsat_formula *f = nullptr;
     int device = 0;
     int32_t slots = 0;
+    int32_t active = 0;                // slots the launches use (0: all)
     int64_t n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
     bcp::VarRec *vr = nullptr;
     uint32_t *cst = nullptr, *epoch = nullptr;
@@ -976,7 +987,7 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
     d.m_pad = b->m_pad;
     d.arena_cap = b->arena_cap;
     d.impl_cap = b->impl_cap;
-    d.n_slots = std::min<int32_t>(b->slots, std::max<int32_t>(n_trails, 1));
+    d.n_slots = std::min<int32_t>(b->active > 0 ? b->active : b->slots, std::max<int32_t>(n_trails, 1));
     d.trail = trail;
     d.toff = toff;
     d.n_trails = n_trails;
@@ -1086,6 +1097,14 @@ extern "C" int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *devic
     if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
     if (slots) *slots = b->slots;
     if (device_bytes) *device_bytes = b->bytes;
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n)
+{
+    if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
+    if (n < 0 || n > b->slots) return set_error(GPSAT_ERR_ARG, "gpsat_bcp_set_active_slots: n outside 0..slots");
+    b->active = n;
     return GPSAT_OK;
 }
 

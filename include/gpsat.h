@@ -131,6 +131,12 @@ int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *t
                        int32_t *impl_reason, int64_t *counters);
 /* Trails in flight and the device bytes the workspace holds. */
 int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
+/* Runs that follow use at most n of the workspace's slots (1 <= n <= slots;
+ * 0 = all).  Outputs do not depend on it.  A launch lasts as long as its
+ * longest trails, which wait on memory the other trails also load: with
+ * trails of very unequal length fewer trails in flight can finish sooner,
+ * with equal ones all slots can (no counterpart in the reference). */
+int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n);
 
 /* Allocation-free BCP (no counterpart in the reference, whose BCP allocates
  * its watch-node pool and graph up front): the same kernel and outputs as

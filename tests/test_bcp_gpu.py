@@ -82,6 +82,26 @@ def test_bcp_slot_reuse_and_epoch_wrap(gpsat, orc, cuda_ok):
     compare_bcp(g, o, label="slot reuse")
 
 
+def test_bcp_active_slots_do_not_change_outputs(gpsat, orc, cuda_ok):
+    # fewer trails in flight than allocated slots (and the ordering kernels
+    # that come with more trails than active slots): same outputs
+    n = 3000
+    lits, off = gpsat.gen_random_ksat(16, n, 12600, 3)
+    tl, to = gpsat.gen_trails(17, n, 200, 0.01, 0.08)
+    f = gpsat.Formula(lits, off, n)
+    b = gpsat.BCPBatch(f, max_slots=64, impl_cap=n)
+    full = b.run_host(tl, to)
+    for k in (5, 1, 0):
+        b.set_active_slots(k)
+        compare_bcp(b.run_host(tl, to), full, label=f"active slots {k}")
+    for bad in (-1, 65):
+        with pytest.raises(gpsat.GpsatError) as e:
+            b.set_active_slots(bad)
+        assert e.value.code == -1
+    o = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=n)
+    compare_bcp(full, o, label="oracle")
+
+
 def test_bcp_capacity_overflow_is_reported(gpsat, orc, cuda_ok):
     n = 2000
     lits, off = gpsat.gen_random_ksat(14, n, 8400, 3)
