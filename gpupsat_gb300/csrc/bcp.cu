@@ -349,12 +349,17 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             props++;
             cur_counted = true;
         }
+        // The scans that come next if the current one implies nothing are the
+        // following trail scans when it is a trail scan, or when it is the
+        // last implication of a trail scan's frame (its descent ends with it
+        // and the depth-first walk returns to the trail)
+        const bool then_trail = (depth == 0 && cur_is_trail) || (depth == 1 && !cur_is_trail && top_j >= top_e);
         if (cur_dp < 0 && cur_wk >= cur_wend) {
-            // scan finished.  A trail scan that implied nothing leads straight
-            // to the next trail scans: this round's window is those alone (as
-            // look-ahead scans, set up from the look-ahead buffer with their
+            // scan finished.  One that implied nothing and is followed by trail
+            // scans leads straight to them: this round's window is those alone
+            // (as look-ahead scans, set up from the look-ahead buffer with their
             // list heads loaded in the round's own trip), not a separate setup
-            const bool next_trail_scans = depth == 0 && cur_is_trail && n_impl == cur_impl_start && ti < tn;
+            const bool next_trail_scans = then_trail && n_impl == cur_impl_start && ti < tn;
             if (!next_trail_scans) {
                 // descend into the implications it found
                 in_scan = false;
@@ -413,7 +418,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         int nsc = 1;
         int my_scan = 0;
         const bool scan0_full = dyn_done && (cur_wk + (uint32_t)take0 == cur_wend);
-        if (scan0_full && depth == 0 && cur_is_trail && n_impl == cur_impl_start && nent < 32 && ti < tn) {
+        if (scan0_full && then_trail && n_impl == cur_impl_start && nent < 32 && ti < tn) {
             // following trail scans, assumed to start with an empty added list
             // (checked in the evaluation trip)
             const int room = 32 - nent;
@@ -809,6 +814,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             dfs_trail = cur_trail;
             ti += new_cur;
             cur_is_trail = true;
+            depth = 0;  // a descent whose scan led into trail scans has ended
             cur_impl_start = n_impl - __popc(imask);
         }
         if (cmask) {
