@@ -109,6 +109,7 @@ struct WarpSmem {
     int32_t sc_end[33];
     uint32_t sc_wk[33];
     uint32_t sc_wend[33];
+    uint8_t q2j[1024];      // look-ahead buffer: entry stream offset -> buffer position
 };
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -280,10 +281,15 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     int32_t cur_var = 0, cur_dp = -1;
     uint32_t cur_wk = 0, cur_wend = 0;
     // look-ahead buffer: lane j holds trail position lb_base + j (its variable
-    // and initial watch-list range), refilled when fewer than 16 lie ahead
+    // and initial watch-list range; positions past the trail: empty).  When
+    // fewer than 16 lie ahead it advances by 16 from values loaded one advance
+    // earlier: lanes 0-15 of nx_* hold positions lb_base + 32.. (their list
+    // ranges in flight) and nnx the trail literals of lb_base + 48.., so an
+    // advance waits on no load.
     int64_t lb_base = INT64_MIN / 2;
-    int32_t lb_v = 0;
-    uint32_t lb_a = 0, lb_b = 0;
+    int32_t lb_v = 0, nx_v = 0, nnx = 0;
+    uint32_t lb_a = 0, lb_b = 0, nx_a = 0, nx_b = 0;
+    int lb_p = 0;
     // every iteration finishes a scan, pops a frame or commits at least one
     // entry; the budget only guarantees termination if that were ever broken
     int64_t budget = MAX_ITERS;
@@ -422,22 +428,71 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             // following trail scans, assumed to start with an empty added list
             // (checked in the evaluation trip)
             const int room = 32 - nent;
-            if (lb_base + 32 - ti < 16 && lb_base + 32 < tn) {
-                lb_base = ti;
-                if (ti + lane < tn) {
-                    const int32_t x = d.trail[tb + ti + lane];
-                    lb_v = (x > 0 ? x : -x) - 1;
-                    lb_a = d.w0off[lb_v];
-                    lb_b = d.w0off[lb_v + 1];
-                    // warm L2 with these scans' initial watch entries (up to 32
-                    // each) by one bulk prefetch of the copy engine per scan:
-                    // the rounds of the next 16-32 trail scans gather them
-                    const uint32_t ne = lb_b - lb_a < 32u ? lb_b - lb_a : 32u;
-                    if (ne > 0)
-                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(d.w0ent + 2 * (size_t)lb_a),
-                                     "r"(ne * 32u)
-                                     : "memory");
+            if (ti - lb_base >= 16 && lb_base + 32 < tn) {
+                const int64_t old_base = lb_base;
+                if (ti - lb_base >= 32) {
+                    // (re)fill at ti: the buffer now, the next 16 and the
+                    // trail literals of the 16 after them in flight
+                    lb_base = ti;
+                    lb_v = 0;
+                    lb_a = lb_b = 0;
+                    if (ti + lane < tn) {
+                        const int32_t x = d.trail[tb + ti + lane];
+                        lb_v = (x > 0 ? x : -x) - 1;
+                        lb_a = d.w0off[lb_v];
+                        lb_b = d.w0off[lb_v + 1];
+                    }
+                    nx_v = 0;
+                    nx_a = nx_b = 0;
+                    if (lane < 16 && ti + 32 + lane < tn) {
+                        const int32_t x = d.trail[tb + ti + 32 + lane];
+                        nx_v = (x > 0 ? x : -x) - 1;
+                        nx_a = d.w0off[nx_v];
+                        nx_b = d.w0off[nx_v + 1];
+                    }
+                } else {
+                    // advance by 16: lanes 0-15 take lanes 16-31, lanes 16-31
+                    // the next 16 (loaded one advance ago)
+                    lb_base += 16;
+                    const int sl = (lane + 16) & 31;
+                    const int32_t hv = __shfl_sync(FULL, lb_v, sl), qv = __shfl_sync(FULL, nx_v, sl);
+                    const uint32_t ha = __shfl_sync(FULL, lb_a, sl), qa = __shfl_sync(FULL, nx_a, sl);
+                    const uint32_t hb = __shfl_sync(FULL, lb_b, sl), qb = __shfl_sync(FULL, nx_b, sl);
+                    lb_v = lane < 16 ? hv : qv;
+                    lb_a = lane < 16 ? ha : qa;
+                    lb_b = lane < 16 ? hb : qb;
+                    nx_v = 0;
+                    nx_a = nx_b = 0;
+                    if (lane < 16 && lb_base + 32 + lane < tn) {
+                        nx_v = (nnx > 0 ? nnx : -nnx) - 1;
+                        nx_a = d.w0off[nx_v];
+                        nx_b = d.w0off[nx_v + 1];
+                    }
                 }
+                nnx = 0;
+                if (lane < 16 && lb_base + 48 + lane < tn) nnx = d.trail[tb + lb_base + 48 + lane];
+                // warm L2 with the initial watch entries of the positions that
+                // entered the buffer (a line holds four): the rounds of the
+                // next trail scans gather them
+                if (lb_base + lane >= old_base + 32) {
+                    const uint32_t ne = lb_b - lb_a < 32u ? lb_b - lb_a : 32u;
+                    for (uint32_t q = 0; q < ne; q += 4)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(d.w0ent + 2 * (size_t)(lb_a + q)));
+                }
+                // the buffer's entry stream, laid out once per refill: position
+                // j's (up to 32) entries follow position j-1's; lb_p is the
+                // inclusive prefix of the counts and q2j maps a stream offset
+                // back to its buffer position
+                const int c = (int)(lb_b - lb_a < 32u ? lb_b - lb_a : 32u);
+                int pc = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL, pc, o);
+                    if (lane >= o) pc += y;
+                }
+                lb_p = pc;
+                for (int q = pc - c; q < pc; q++) sm.q2j[q] = (uint8_t)lane;
+                __syncwarp();
             }
             const int lb_off = (int)(ti - lb_base);
             const int64_t ahead = (32 - lb_off < tn - ti) ? (int64_t)(32 - lb_off) : tn - ti;
@@ -445,6 +500,9 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             const int src = (lb_off + lane) & 31;
             const int32_t bv = __shfl_sync(FULL, lb_v, src);
             const uint32_t ba = __shfl_sync(FULL, lb_a, src), bb = __shfl_sync(FULL, lb_b, src);
+            const int bp = __shfl_sync(FULL, lb_p, src);
+            // stream offset of the window's first look-ahead entry
+            const int pbase = lb_off > 0 ? __shfl_sync(FULL, lb_p, (lb_off - 1) & 31) : 0;
             int32_t v = -1;
             uint32_t a = 0, b = 0;
             if (lane < nlook) {
@@ -453,12 +511,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 b = bb;
             }
             const int cnt = (lane < nlook) ? (int)(b - a < 32u ? b - a : 32u) : 0;
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += y;
-            }
+            const int incl = bp - pbase;  // (lanes below nlook)
             const int excl = incl - cnt;
             const unsigned ok = __ballot_sync(FULL, lane < nlook && excl < room);
             const int K = (~ok) ? __ffs(~ok) - 1 : 32;
@@ -471,15 +524,8 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             }
             if (K > 0) {
                 const int total = min(nent + __shfl_sync(FULL, incl, K - 1), 32);
-                // window position -> lookahead scan: rank among the scans that start
-                // at or before it, mapped through the mask of non-empty scans
-                const bool nonempty = lane < K && cnt > 0;
-                const unsigned nem = __ballot_sync(FULL, nonempty);
-                const unsigned starts = __reduce_or_sync(FULL, nonempty ? (1u << (nent + excl)) : 0u);
-                if (lane >= nent && lane < total) {
-                    const int rank = __popc(starts & (lane == 31 ? FULL : ((2u << lane) - 1u)));
-                    my_scan = 1 + nth_set_bit(nem, rank);
-                }
+                // window position -> look-ahead scan, through the stream map
+                if (lane >= nent && lane < total) my_scan = 1 + (int)sm.q2j[pbase + lane - nent] - lb_off;
                 const int jj = my_scan - 1;
                 const int ej = __shfl_sync(FULL, excl, jj < 0 ? 0 : jj);
                 const uint32_t aj = __shfl_sync(FULL, a, jj < 0 ? 0 : jj);
@@ -510,6 +556,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         r.unit = -1;
         r.nw1 = r.nw2 = 0;
         bool valid = false;
+        int32_t ov = -1;  // a valid entry's clause: its other watched variable
         int w1 = 0, w2 = 0;
         uint32_t scan_h = 0;
         if (has) {
@@ -553,6 +600,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                     }
                 }
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
+                if (valid) ov = ((l1 >> 1) == sv) ? (l2 >> 1) : (l1 >> 1);
                 if (valid) {
                     r.acnt = 2;
                     if (!(c1 && c2)) {
@@ -617,6 +665,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             } else {
                 const int32_t l1 = d.lits[en.y + w1], l2 = d.lits[en.y + w2];
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
+                if (valid) ov = ((l1 >> 1) == sv) ? (l2 >> 1) : (l1 >> 1);
                 if (valid) eval_long(d, vr, en.y, len, w1, w2, e, r);
             }
         } else if (scan_v >= 0) {
@@ -626,9 +675,14 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         // ---- where the commit stops: the smallest event key of the round
         int key = NO_CUT;
         {
-            const int keyc = has ? en.x : -1 - lane;
-            const unsigned mm = __match_any_sync(FULL, keyc);
-            if (has && (mm & lt)) key = key_before(lane, my_scan);  // clause seen earlier this round
+            // an entry whose clause an earlier entry of the round also holds
+            // (and may change).  A clause is listed once per variable and only
+            // a valid entry acts, so that is a valid entry whose clause's other
+            // watched variable is an earlier window scan's (scan 0: checked
+            // here; later scans: in the loop below).  Scan 0 may have entries
+            // from earlier rounds, so this can cut where nothing repeats: a
+            // cut only ends the round early.
+            if (valid && my_scan > 0 && ov == cur_var) key = key_before(lane, my_scan);
             if (valid && r.act == A_CONFLICT) key = min(key, key_after(lane, my_scan));
             // an implication ends its scan's part of the window (its depth-first
             // descent comes before any later scan) ...
@@ -651,16 +705,17 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             }
             // a later window scan whose list starts with added clauses
             if (scan_v >= 0 && (scan_h >> 24) == e) key = min(key, key_before(scan_b, lane));
-            // a move of this lane that lands in a later window scan's list
-            // (lane s holds window scan s's variable and start; the loop is
-            // uniform, so its shuffles are independent and overlap, and the
-            // smallest key is the first such scan)
+            // a move of this lane that lands in a later window scan's list, and
+            // the repeated clauses of scans 1.. (lane s holds window scan s's
+            // variable and start; the loop is uniform, so its shuffles are
+            // independent and overlap, and the smallest key is the first scan)
             const bool mv = valid && (r.act == A_SW1 || r.act == A_SW2);
-            if (nsc > 1 && __any_sync(FULL, mv)) {
+            if (nsc > 1) {
                 for (int s = 1; s < nsc; s++) {
                     const int32_t vs = __shfl_sync(FULL, scan_v, s);
                     const int bs = __shfl_sync(FULL, scan_b, s);
                     if (mv && s > my_scan && (vs == r.t1 || vs == r.t2)) key = min(key, key_before(bs, s));
+                    if (valid && s < my_scan && vs == ov) key = min(key, key_before(lane, my_scan));
                 }
             }
         }
