@@ -104,7 +104,7 @@ struct Ctx {
     float *bmax;     // per block of 32 variables: >= the largest activity of its unassigned
                      // variables (-1: none left); exact for a block pick_branch last tightened
     bool use_bmax;   // large formulas pick through the block bounds, small ones scan
-    int32_t *wl_start, *wl_size, *wl_cap, *wl_cnt;
+    int32_t *wl_start, *wl_size, *wl_cap;
     int2 *watches;
     int32_t *arena, *crefs;
     int32_t *sm64;   // 64 ints of shared memory for this warp
@@ -152,28 +152,30 @@ __device__ bool rebuild_watches(Ctx &C)
 {
     const int lane = C.lane;
     const int nl = 2 * C.n;
-    for (int i = lane; i < nl; i += 32) C.wl_cnt[i] = 0;
+    // the list sizes count each literal's watches first; the layout below
+    // reads each count once and then sets the size to zero
+    for (int i = lane; i < nl; i += 32) C.wl_size[i] = 0;
     __syncwarp();
     for (int k = lane; k < C.n_crefs; k += 32) {
         const int32_t r = C.crefs[k];
         const uint32_t h = (uint32_t)C.arena[r];
         if (!(h & F_DELETED) && (h & LEN_MASK) >= 2) {
-            atomicAdd(&C.wl_cnt[C.arena[r + HDR]], 1);
-            atomicAdd(&C.wl_cnt[C.arena[r + HDR + 1]], 1);
+            atomicAdd(&C.wl_size[C.arena[r + HDR]], 1);
+            atomicAdd(&C.wl_size[C.arena[r + HDR + 1]], 1);
         }
     }
     __syncwarp();
     // half the spare capacity at most is shared out in proportion to each
     // list's length plus one; the other half is the free tail
     int64_t total = 0;
-    for (int i = lane; i < nl; i += 32) total += C.wl_cnt[i];
+    for (int i = lane; i < nl; i += 32) total += C.wl_size[i];
     total = wsum(total);
     if (total > C.WCAP) return false;
     const int64_t spare = C.WCAP - total, weight = 2 * (total + nl);
     int64_t running = 0;
     for (int b = 0; b < nl; b += 32) {
         const int i = b + lane;
-        const int c = i < nl ? C.wl_cnt[i] : 0;
+        const int c = i < nl ? C.wl_size[i] : 0;
         const int room = min((int)(spare * (c + 1) / weight), c / 2 + 8);
         const int cap = i < nl ? c + room : 0;
         const int incl = wscan_incl(cap, lane);
@@ -1294,14 +1296,13 @@ __device__ __forceinline__ void cdcl_body(const Params &P)
         C.reason = (int32_t *)carve(4 * N);
         C.trail = (int32_t *)carve(4 * N);
         C.act = (float *)carve(4 * N);
-        C.bmax = (float *)carve(4 * (N / 16));
-        C.tlim = (int32_t *)carve(4 * (N + 16));
-        C.learnt = (int32_t *)carve(4 * (N + 16));
-        C.lstamp = (int32_t *)carve(4 * (N + 16));
+        C.bmax = nullptr;  // block bounds: formulas above 1024 variables only
+        C.tlim = (int32_t *)carve(4 * (N + 4));
+        C.learnt = (int32_t *)carve(4 * (N + 4));
+        C.lstamp = (int32_t *)carve(4 * (N + 4));
         C.wl_start = (int32_t *)carve(8 * N);
         C.wl_size = (int32_t *)carve(8 * N);
         C.wl_cap = (int32_t *)carve(8 * N);
-        C.wl_cnt = (int32_t *)carve(8 * N);
         C.val = (int8_t *)carve(N);
         C.phase = (int8_t *)carve(N);
         C.seen = (uint8_t *)carve(N);
@@ -1320,7 +1321,6 @@ __device__ __forceinline__ void cdcl_body(const Params &P)
         C.wl_start = P.wl_start + S * 2 * N;
         C.wl_size = P.wl_size + S * 2 * N;
         C.wl_cap = P.wl_cap + S * 2 * N;
-        C.wl_cnt = P.wl_cnt + S * 2 * N;
     }
     C.watches = P.watches + S * (size_t)P.WCAP;
     C.arena = P.arena + S * (size_t)P.ACAP;
@@ -1361,10 +1361,11 @@ __device__ __forceinline__ void cdcl_body(const Params &P)
     }
 }
 
-// Two register targets: 4 blocks/SM (128 registers) when the per-variable
-// arrays sit in HBM, 3 (about 160) when they sit in shared memory, which four
-// blocks of N > 240 variables would not fit.
+// Three builds: 4 blocks/SM (128 registers) with the per-variable arrays in
+// HBM; in shared memory, 4 blocks/SM when four blocks of them fit (N up to
+// about 250) and 3 (about 160 registers) when only three do (N up to about 290).
 __global__ void __launch_bounds__(WARPS * 32, 3) cdcl_kernel_smem(Params P) { cdcl_body(P); }
+__global__ void __launch_bounds__(WARPS * 32, 4) cdcl_kernel_smem4(Params P) { cdcl_body(P); }
 __global__ void __launch_bounds__(WARPS * 32, 4) cdcl_kernel_hbm(Params P) { cdcl_body(P); }
 
 }  // namespace cdcl

@@ -39,13 +39,14 @@ struct Opts {
 };
 
 // Bytes of shared memory one warp needs to hold its job's per-variable and
-// per-literal arrays for N variables (N a multiple of 16): level, reason,
-// trail, activity (4N each); tlim, learnt, lstamp (4(N+16) each); the four
-// watch-list header arrays (8N each); the activity bound per block of 32
-// variables (4 N/16); value, phase, seen (N each); rounded up to 16 bytes.
+// per-literal arrays for N variables (N a multiple of 4): level, reason,
+// trail, activity (4N each); tlim, learnt, lstamp (4(N+4) each); the three
+// watch-list header arrays start, size, capacity (8N each); value, phase,
+// seen (N each); rounded up to 16 bytes.  (The activity block bounds serve
+// formulas above 1024 variables, far more than shared memory holds.)
 constexpr int64_t smem_bytes_per_warp(int64_t N)
 {
-    return (16 * N + 12 * (N + 16) + 32 * N + 4 * (N / 16) + 3 * N + 15) / 16 * 16;
+    return (16 * N + 12 * (N + 4) + 24 * N + 3 * N + 15) / 16 * 16;
 }
 
 struct Params {
@@ -80,7 +81,7 @@ struct Params {
     int32_t *level, *reason, *trail, *tlim, *learnt, *lstamp, *tmp;
     float *act;
     float *bmax;                 // per slot N/16 floats: activity bound per block of 32 variables
-    int32_t *wl_start, *wl_size, *wl_cap, *wl_cnt;
+    int32_t *wl_start, *wl_size, *wl_cap;
     int2 *watches;
     int32_t *arena, *crefs;
 };

@@ -25,8 +25,11 @@
 namespace gpsat {
 namespace cdcl {
 __global__ void cdcl_kernel_smem(Params P);
+__global__ void cdcl_kernel_smem4(Params P);
 __global__ void cdcl_kernel_hbm(Params P);
 }
+// which build of the solver kernel a workspace runs
+enum : int { K_HBM = 0, K_SMEM3 = 1, K_SMEM4 = 2 };
 
 namespace {
 
@@ -101,7 +104,7 @@ struct gpsat_batch {
     // workspace
     cdcl::Params P{};
     int64_t ws_bytes = 0;
-    int32_t ws_slots = 0, ws_N = 0, minb = 3;
+    int32_t ws_slots = 0, ws_N = 0, kind = gpsat::K_SMEM3;  // build of the solver kernel
     int64_t ws_W = 0, ws_A = 0, ws_C = 0;
     void *ws = nullptr;
     int max_len = 0, max_m = 0;
@@ -134,7 +137,8 @@ void batch_free(gpsat_batch *b)
 // Workspace sized for the largest formula of the batch.
 int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
 {
-    const int32_t N = (int32_t)((*std::max_element(b->n_vars.begin(), b->n_vars.end()) + 15) / 16 * 16);
+    // (a multiple of 4: the shared-memory arrays stay 16-byte aligned)
+    const int32_t N = (int32_t)((*std::max_element(b->n_vars.begin(), b->n_vars.end()) + 3) / 4 * 4);
     const int64_t lfirst = std::max<int64_t>(o->learnt_first, b->max_m / 2);
     const int64_t C = b->max_m + 3 * lfirst + 4 * (int64_t)o->learnt_inc + N + 64;
     // a multiple of 4 words: every slot's arena starts 16-byte aligned (the
@@ -144,41 +148,43 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     int sms = 0, per_sm = 0, smem_max = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
-    // Two builds of the kernel: 3 blocks/SM with the per-variable arrays in
-    // shared memory when three blocks of them fit (no fewer resident blocks
-    // than its registers allow), else 4 blocks/SM with them in HBM.
+    // Three builds of the kernel: with the per-variable arrays in shared
+    // memory, 4 blocks/SM when four blocks of them fit and 3 when three do (no
+    // fewer resident blocks than each build's registers allow); else 4
+    // blocks/SM with the arrays in HBM.
     int32_t smem_warp = (int32_t)cdcl::smem_bytes_per_warp(N);
-    int minb = 3;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel_smem, 128, 0);
+    int kind = K_HBM;
     if (4 * (int64_t)smem_warp + 1024 > smem_max) smem_warp = 0;
     if (smem_warp > 0) {
-        int per_sm_smem = 0;
-        if (cudaFuncSetAttribute(cdcl::cdcl_kernel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 4 * smem_warp) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_smem, cdcl::cdcl_kernel_smem, 128, 4 * smem_warp) !=
-                cudaSuccess ||
-            per_sm_smem < per_sm) {
+        for (int k : {K_SMEM4, K_SMEM3}) {
+            const void *fn = k == K_SMEM4 ? (const void *)cdcl::cdcl_kernel_smem4 : (const void *)cdcl::cdcl_kernel_smem;
+            int by_regs = 0, with_smem = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by_regs, fn, 128, 0) == cudaSuccess &&
+                cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * smem_warp) == cudaSuccess &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&with_smem, fn, 128, 4 * smem_warp) == cudaSuccess &&
+                with_smem >= by_regs && by_regs >= (k == K_SMEM4 ? 4 : 3)) {
+                kind = k;
+                per_sm = with_smem;
+                break;
+            }
             cudaGetLastError();
-            smem_warp = 0;
         }
+        if (kind == K_HBM) smem_warp = 0;
     }
-    if (smem_warp == 0) {
-        minb = 4;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel_hbm, 128, 0);
-    }
+    if (kind == K_HBM) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cdcl::cdcl_kernel_hbm, 128, 0);
     int32_t slots = o->max_slots > 0 ? o->max_slots : std::max(1, sms * std::max(per_sm, 1) * 4);
     // per-variable arrays in HBM only when they are not in shared memory
     const int64_t NV = smem_warp > 0 ? 0 : N;
     const int64_t per_slot =
-        NV * (1 + 1 + 1 + 4 * 4) + 3 * (NV + 1) * 4 + 4 * 2 * NV * 4 + 4 * (NV / 16) + W * 8 + A * 4 + C * 8;
+        NV * (1 + 1 + 1 + 4 * 4) + 3 * (NV + 1) * 4 + 3 * 2 * NV * 4 + 4 * (NV / 16) + W * 8 + A * 4 + C * 8;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const int64_t budget = (int64_t)((free_b + (size_t)b->ws_bytes) * 0.5);
     if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
     if (b->ws && slots == b->ws_slots && N == b->ws_N && W == b->ws_W && A == b->ws_A && C == b->ws_C &&
-        smem_warp == b->P.smem_per_warp && minb == b->minb)
+        smem_warp == b->P.smem_per_warp && kind == b->kind)
         return GPSAT_OK;
-    b->minb = minb;
+    b->kind = kind;
     cudaFree(b->ws);
     b->ws = nullptr;
     const size_t S = slots;
@@ -193,7 +199,7 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
            o_learnt = take(S * (NV + 1) * 4), o_lstamp = take(S * (NV + 1) * 4), o_act = take(S * NV * 4),
            o_bmax = take(S * (NV / 16) * 4),
            o_ws = take(S * 2 * NV * 4), o_wz = take(S * 2 * NV * 4), o_wc = take(S * 2 * NV * 4),
-           o_wn = take(S * 2 * NV * 4), o_w = take(S * W * 8), o_a = take(S * A * 4), o_c = take(S * C * 4),
+           o_w = take(S * W * 8), o_a = take(S * A * 4), o_c = take(S * C * 4),
            o_t = take(S * C * 4);
     if (cudaMalloc(&b->ws, off) != cudaSuccess) {
         cudaGetLastError();
@@ -215,7 +221,6 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     P.wl_start = (int32_t *)(base + o_ws);
     P.wl_size = (int32_t *)(base + o_wz);
     P.wl_cap = (int32_t *)(base + o_wc);
-    P.wl_cnt = (int32_t *)(base + o_wn);
     P.watches = (int2 *)(base + o_w);
     P.arena = (int32_t *)(base + o_a);
     P.crefs = (int32_t *)(base + o_c);
@@ -505,8 +510,10 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (J) {
         const int slots = std::min<int32_t>(b->ws_slots, J);
         P.n_slots = slots;
-        if (b->minb == 4)
+        if (b->kind == K_HBM)
             cdcl::cdcl_kernel_hbm<<<(slots + 3) / 4, 128, 0, st>>>(P);
+        else if (b->kind == K_SMEM4)
+            cdcl::cdcl_kernel_smem4<<<(slots + 3) / 4, 128, 4 * (size_t)P.smem_per_warp, st>>>(P);
         else
             cdcl::cdcl_kernel_smem<<<(slots + 3) / 4, 128, 4 * (size_t)P.smem_per_warp, st>>>(P);
         P.n_slots = b->ws_slots;
