@@ -1195,6 +1195,34 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
     const int64_t nl = trail_offsets[n_trails];
     if (nl < 0 || (nl > 0 && !trail_lits)) return set_error(GPSAT_ERR_ARG, "bad trail offsets");
+    {
+        // Every buffer page-locked (cudaHostAlloc / cudaHostRegister, as
+        // torch's pin_memory): the kernel reads the trails and writes the
+        // results in place, over the CPU-GPU link, with no staging copies.
+        const void *hp[9] = {nl > 0 ? (const void *)trail_lits : (const void *)trail_offsets, trail_offsets, status, conflict_clause, stop_index,
+                             n_impl, impl_lit, impl_reason, counters ? (const void *)counters : trail_offsets};
+        void *dp[9];
+        bool all = true;
+        for (int i = 0; i < 9 && all; i++) {
+            cudaPointerAttributes a;
+            if (cudaPointerGetAttributes(&a, hp[i]) != cudaSuccess) {
+                cudaGetLastError();
+                all = false;
+            } else {
+                all = a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+                dp[i] = a.devicePointer;
+            }
+        }
+        if (all) {
+            int rc = launch(b, (const int32_t *)dp[0], (const int64_t *)dp[1], n_trails, (int32_t *)dp[2],
+                            (int32_t *)dp[3], (int32_t *)dp[4], (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7],
+                            counters ? (int64_t *)dp[8] : nullptr, 0);
+            if (rc != GPSAT_OK) return rc;
+            err = cudaStreamSynchronize(0);
+            if (err != cudaSuccess) return cuda_error(err, "bcp run");
+            return GPSAT_OK;
+        }
+    }
     if (nl > b->trail_cap) {
         cudaFree(b->d_trail);
         b->d_trail = nullptr;

@@ -124,7 +124,11 @@ int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, const int64_t 
                          int32_t n_trails, int32_t *status, int32_t *conflict_clause,
                          int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,
                          int32_t *impl_reason, int64_t *counters, void *stream);
-/* Host pointers: copies the trails in, runs, copies the results out, waits. */
+/* Host pointers: copies the trails in, runs, copies the results out, waits.
+ * When every buffer is page-locked host memory (cudaHostAlloc, cudaHostRegister,
+ * torch's pin_memory) the kernel reads the trails and writes the results in
+ * place over the CPU-GPU link instead, with no staging copies; the results are
+ * the same. */
 int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
                        int32_t n_trails, int32_t *status, int32_t *conflict_clause,
                        int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,

@@ -145,6 +145,27 @@ def test_bcp_device_entry_matches_host_entry(gpsat, cuda_ok):
     assert np.array_equal(d["counters"], h["counters"])
 
 
+def test_bcp_pinned_host_buffers_in_place(gpsat, cuda_ok):
+    # page-locked inputs and outputs are used in place by the kernel: same
+    # results as the staged (pageable) path
+    import torch
+    n = 5000
+    lits, off = gpsat.gen_random_ksat(23, n, 21000, 3)
+    tl, to = gpsat.gen_trails(24, n, 300, 0.01, 0.05)
+    b = gpsat.BCPBatch(gpsat.Formula(lits, off, n), impl_cap=512)
+    h = b.run_host(tl, to)
+    tdt = {np.int32: torch.int32, np.int64: torch.int64}
+    pinned = lambda shape, dt: torch.zeros(shape, dtype=tdt[dt], pin_memory=True).numpy()
+    p_tl, p_to = pinned(tl.shape, np.int32), pinned(to.shape, np.int64)
+    p_tl[:] = tl
+    p_to[:] = to
+    out = b.host_outputs(len(to) - 1, counters=True, alloc=pinned)
+    for _ in range(2):
+        p = b.run_host(p_tl, p_to, out=out)
+        compare_bcp(p, h, label="pinned in place")
+        assert np.array_equal(p["counters"], h["counters"])
+
+
 def test_bcp_full_size_benchmark_shape(gpsat, orc, cuda_ok):
     """n=1e6, m=4.2e6, 4096 trails at 1-5%: a seeded sample of 96 trails is
     compared bit-exactly with the oracle; every trail's outputs are checked for
