@@ -52,6 +52,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cstdio>
 #include <mutex>
 
@@ -75,6 +76,7 @@ struct VarRec {
     uint8_t asg;       // (epoch<<1)|sign: trail literal or pending implication
     uint8_t pad[3];
 };
+static_assert(sizeof(VarRec) == 8 && offsetof(VarRec, asg) == 4, "the assignment byte starts a 4-byte word");
 
 struct Dev {
     int32_t n_vars;
@@ -251,26 +253,25 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
     const int64_t tb = d.toff[t];
     const int64_t tn = d.toff[t + 1] - tb;
 
-    // ---- assign every trail literal first
+    // ---- assign every trail literal first, in one pass: an exchange on the
+    // word that holds the assignment byte (the rest of the word is padding)
+    // returns what was there, and the same variable given the other sign
+    // earlier in this trail (by any lane) shows as this epoch's opposite sign
     bool bad = tn < 0;
     // (unrolled so that several iterations' loads are in flight at once)
 #pragma unroll 4
     for (int64_t i = lane; i < tn; i += 32) {
-        int32_t x = d.trail[tb + i];
-        if (x == 0 || x > n || x < -n) bad = true;
-        else vr[(x > 0 ? x : -x) - 1].asg = (uint8_t)((e << 1) | (x > 0 ? 1u : 0u));
+        const int32_t x = d.trail[tb + i];
+        if (x == 0 || x > n || x < -n) {
+            bad = true;
+        } else {
+            const unsigned a = (e << 1) | (x > 0 ? 1u : 0u);
+            const unsigned old = atomicExch(reinterpret_cast<unsigned *>(&vr[(x > 0 ? x : -x) - 1].asg), a) & 0xFFu;
+            if ((old >> 1) == e && old != a) bad = true;
+        }
     }
     bad = __any_sync(FULL, bad);
     __syncwarp();
-    if (!bad) {
-        // a variable given both signs leaves one of its literals unmatched
-#pragma unroll 4
-        for (int64_t i = lane; i < tn; i += 32) {
-            int32_t x = d.trail[tb + i];
-            if (vr[(x > 0 ? x : -x) - 1].asg != (uint8_t)((e << 1) | (x > 0 ? 1u : 0u))) bad = true;
-        }
-        bad = __any_sync(FULL, bad);
-    }
 
     int64_t n_impl = 0, props = 0, cI = 0;
     int64_t myW = 0, myL = 0, myA = 0;  // lane-private, reduced at the end
