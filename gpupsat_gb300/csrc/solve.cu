@@ -134,8 +134,8 @@ void batch_free(gpsat_batch *b)
     for (void *p : ptrs) cudaFree(p);
 }
 
-// Workspace sized for the largest formula of the batch.
-int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
+// Workspace sized for the largest formula of the batch and a launch of J jobs.
+int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o, int32_t J)
 {
     // (a multiple of 4: the shared-memory arrays stay 16-byte aligned)
     const int32_t N = (int32_t)((*std::max_element(b->n_vars.begin(), b->n_vars.end()) + 3) / 4 * 4);
@@ -151,12 +151,16 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
     // Three builds of the kernel: with the per-variable arrays in shared
     // memory, 4 blocks/SM when four blocks of them fit and 3 when three do (no
     // fewer resident blocks than each build's registers allow); else 4
-    // blocks/SM with the arrays in HBM.
+    // blocks/SM with the arrays in HBM.  The 4-block build leaves L1 little
+    // room beside four blocks' shared memory, so it is the first choice only
+    // for a launch with more jobs than three blocks per SM hold.
     int32_t smem_warp = (int32_t)cdcl::smem_bytes_per_warp(N);
     int kind = K_HBM;
     if (4 * (int64_t)smem_warp + 1024 > smem_max) smem_warp = 0;
     if (smem_warp > 0) {
-        for (int k : {K_SMEM4, K_SMEM3}) {
+        const bool many = (int64_t)J > (int64_t)sms * 3 * 4;
+        const int order[2] = {many ? K_SMEM4 : K_SMEM3, many ? K_SMEM3 : K_SMEM4};
+        for (int k : order) {
             const void *fn = k == K_SMEM4 ? (const void *)cdcl::cdcl_kernel_smem4 : (const void *)cdcl::cdcl_kernel_smem;
             int by_regs = 0, with_smem = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by_regs, fn, 128, 0) == cudaSuccess &&
@@ -164,7 +168,7 @@ int ensure_workspace(gpsat_batch *b, const gpsat_solve_options *o)
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&with_smem, fn, 128, 4 * smem_warp) == cudaSuccess &&
                 with_smem >= by_regs && by_regs >= (k == K_SMEM4 ? 4 : 3)) {
                 kind = k;
-                per_sm = with_smem;
+                per_sm = by_regs;  // (shared memory allows at least as many)
                 break;
             }
             cudaGetLastError();
@@ -428,7 +432,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         for (int32_t f = 0; f < F; f++) add_job(f, nullptr, 0);
     }
     const int32_t J = (int32_t)jinst.size();
-    int rc = ensure_workspace(b, &o);
+    int rc = ensure_workspace(b, &o, J);
     if (rc != GPSAT_OK) return rc;
     if (J > b->job_cap) {
         cudaFree(b->d_job_inst);
