@@ -20,9 +20,24 @@ literals in order, reason clauses, conflict flag / clause, stop index.
   cpu_baseline  the oracle's C restatement of the reference BCP (same
           semantics and outputs) on the host cores, on a bounded sample
 
-`--impl reference` times the reference-semantics CPU path alone.  Under
-torchrun each rank runs its own 4096 trails (weak scaling; trails never
-exchange data) and rank 0 prints one JSON line.
+Beside the BCP figures the default line carries two more measurements of the
+same run (each skipped with --no-solve / --no-latency):
+  solve     the batched solve workload: 16,384 seeded random 3-SAT instances,
+            n ~ U[50, 250], m = round(4.26 n), one persistent launch, 10^5
+            conflicts per instance; decided instances/s, verdict counts, every
+            SAT model checked on the device and on the host, and the verdicts
+            compared with the reference's own (recorded in tests/golden)
+  latency   single-instance solving: 40 seeded n=50, m=213 instances, one
+            solve call each; milliseconds per call
+
+`--impl reference` times the reference's CPU path alone: the BCP restatement
+on all host cores, its own solver (host build, iteration cap lifted, a wall
+budget per instance, one process per core) on a sample of the solve
+workload, its own solver per single instance on one core, and its own BCP at
+a scaled-down n.  Its inputs come from the oracle's generator, so that arm
+loads nothing of the shipped library.  Under torchrun each rank runs its own
+4096 trails (weak scaling; trails never exchange data) and rank 0 prints one
+JSON line.
 """
 from __future__ import annotations
 
@@ -75,13 +90,24 @@ def parse():
     ap.add_argument("--instances", type=int, default=None, help="solve: 16384, planted: 128, seeding: 1024 held-out formulas")
     ap.add_argument("--depth", default="6", help="planted: split variables per instance (cubes = 2^depth), "
                                                  "or 'auto' to autotune it on a sample")
-    ap.add_argument("--cpu-instances", type=int, default=64)
-    ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    ap.add_argument("--cpu-instances", type=int, default=256,
+                    help="reference solve sample: the first N instances of the solve workload")
+    ap.add_argument("--cpu-seconds", type=float, default=60.0, help="reference solve sample: wall budget")
+    ap.add_argument("--ref-budget", type=float, default=5.0,
+                    help="reference solve sample: wall seconds per instance before it counts as ref-undecided")
+    ap.add_argument("--no-solve", action="store_true", help="bcp: leave out the batched-solve measurement")
+    ap.add_argument("--no-latency", action="store_true", help="bcp: leave out the single-instance measurement")
+    ap.add_argument("--solve-instances", type=int, default=16384, help="bcp: instances of the solve measurement")
     return ap.parse_args()
 
 
-def workload(args, rank):
-    import gpupsat_gb300 as g
+def workload(args, rank, gen=None):
+    """The BCP workload; gen is the module whose generators make it (the
+    library's by default; the oracle's restatement of the same streams for the
+    reference arm)."""
+    if gen is None:
+        import gpupsat_gb300 as gen
+    g = gen
     n = args.n_vars
     m = int(round(args.ratio * n))
     lits, off = g.gen_random_ksat(2024, n, m, 3)
@@ -184,7 +210,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    n, m, lits, off, tl, to = workload(args, 0)
+    import oracle
+    n, m, lits, off, tl, to = workload(args, 0, gen=oracle)
     threads = os.cpu_count() or 1
     vals = []
     per_step = max(64, min(args.cpu_trails, args.trails))
@@ -209,7 +236,52 @@ def run_reference(args):
                                        f"BCP cannot hold n=1e6 (100k-node watch pool, O(n) per assignment), so "
                                        f"its C restatement (oracle/bcp_ref.c, bit-exact with it) is timed"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["cpu_baseline"]["ref_own_scaled"] = ref_own_bcp_scaled()
+    if not args.no_solve:
+        line["solve"] = solve_object_ref(args)
+    if not args.no_latency:
+        line["latency"] = latency_object_ref()
     print(json.dumps(line))
+
+
+def _ref_lib(variant):
+    import ctypes
+    import platform
+    from oracle.ref import build_ref
+    L = ctypes.CDLL(str(build_ref.OUT / f"libref_{variant}_{platform.machine()}.so"))
+    vp = ctypes.c_void_p
+    L.ref_solve.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64, vp]
+    L.ref_solve.restype = ctypes.c_int
+    L.ref_bcp_timed.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int64] + [vp] * 6
+    L.ref_bcp_timed.restype = ctypes.c_int
+    return L
+
+
+def ref_own_bcp_scaled(n=2000, trails=1024):
+    """The reference's own BCP (its WatchedClausesList, host build) at a
+    scaled-down size of the BCP workload: n=2000, m=8400, trails of 1-5% of
+    the variables, one host core, one call per trail; the time is that of the
+    trail application alone (the driver times the assignments and the
+    new_decision calls, not the watch-list set-up before them)."""
+    import oracle
+    L = _ref_lib("stock")
+    m = int(round(4.2 * n))
+    lits, off = oracle.gen_random_ksat(2024, n, m, 3)
+    tl, to = oracle.gen_trails(7, n, trails, 0.01, 0.05)
+    props = int(oracle.BCPOracle(lits, off, n).run(tl, to, impl_cap=n)["counters"][:, 0].sum())
+    a, b = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    k1, c1, s1 = np.zeros(1, np.int64), np.zeros(1, np.int32), np.zeros(1, np.int32)
+    sec = np.zeros(1, np.float64)
+    P = lambda x: x.ctypes.data
+    total = 0.0
+    for t in range(trails):
+        tr = np.ascontiguousarray(tl[to[t]:to[t + 1]])
+        L.ref_bcp_timed(P(lits), P(off), n, m, P(tr), len(tr), n, P(a), P(b), P(k1), P(c1), P(s1), P(sec))
+        total += float(sec[0])
+    return {"value": props / total, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": f"n={n}, m={m}, {trails} trails of 1-5% ({props} propagations, {total:.2f} s): the "
+                      f"reference's own WatchedClausesList (host build), one call per trail, trail application "
+                      f"timed alone"}
 
 
 def combine_ranks(dist, device, seconds, units):
@@ -330,99 +402,287 @@ def run_gpu(args):
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"first {Tc} of the {T} trails ({props} propagations, {dt:.1f} s); oracle/bcp_ref.c, "
                          f"the reference's BCP semantics restated (bit-exact with it)"}
+    check = bcp_sample_check(out, lits, off, n, tl, to, cap)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
-            "config": {**config(args, n, m), "slots": active,
+            "config": config(args, n, m),
+            "launch": {"slots": active,
                        "slot_tuning_ms": {str(k): round(v, 3) for k, v in tuning.items()} if tuning else None},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": args.steps * (4 if T > active else 1),  # order kernels + BCP kernel
-            "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item())}
+            "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item()),
+            "check": check}
+    del out, d_tl, d_to
+    b.close()
+    f.close()
+    torch.cuda.empty_cache()
+    if not args.no_solve:
+        line["solve"] = solve_object_gpu(args, args.solve_instances)
+    if not args.no_latency:
+        line["latency"] = latency_object_gpu(args)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def bcp_sample_check(out, lits, off, n, tl, to, cap, k=64):
+    """Compares k evenly spaced trails of the last timed launch's outputs with
+    the oracle, bit for bit (status, conflict clause, stop index, implied
+    literals and reasons in order, counters); raises on a difference."""
+    import oracle
+    T = len(to) - 1
+    idx = np.unique(np.linspace(0, T - 1, min(k, T)).astype(np.int64))
+    sub_to = np.zeros(len(idx) + 1, np.int64)
+    sub_to[1:] = np.cumsum(to[idx + 1] - to[idx])
+    sub_tl = np.concatenate([tl[to[i]:to[i + 1]] for i in idx])
+    ref = oracle.BCPOracle(lits, off, n).run(sub_tl, sub_to, impl_cap=cap, threads=os.cpu_count() or 1)
+    got = {key: out[key].cpu().numpy()[idx] for key in ("status", "conflict", "stop", "n_impl", "counters")}
+    for key in ("status", "conflict", "stop", "n_impl", "counters"):
+        if not np.array_equal(got[key], ref[key]):
+            raise AssertionError(f"bench check: BCP {key} differs from the oracle on the timed launch")
+    il = out["impl_lit"].cpu().numpy()[idx]
+    ir = out["impl_reason"].cpu().numpy()[idx]
+    for j in range(len(idx)):
+        kk = int(ref["n_impl"][j])
+        if not (np.array_equal(il[j, :kk], ref["impl_lit"][j, :kk]) and
+                np.array_equal(ir[j, :kk], ref["impl_reason"][j, :kk])):
+            raise AssertionError(f"bench check: implications of trail {int(idx[j])} differ from the oracle")
+    return {"trails": int(len(idx)), "bit_exact": True, "against": "oracle/bcp_ref.c",
+            "propagations": int(ref["counters"][:, 0].sum())}
 
 
 # ---------------------------------------------------------------- batched solving
 SOLVE_METRIC = "instances decided/s"
 
 
-def solve_instances(count, first=0, n_range=(50, 250)):
+def solve_instances(count, first=0, n_range=(50, 250), gen=None):
     """Seeded random 3-SAT, n ~ U[n_range], m = round(4.26 n): instance i uses
     formula seed 5000 + i; the sizes come from one seeded stream."""
-    import gpupsat_gb300 as g
+    if gen is None:
+        import gpupsat_gb300 as gen
     ns = np.random.default_rng(11).integers(n_range[0], n_range[1] + 1, size=first + count)[first:]
-    return [(int(n), *g.gen_random_ksat(5000 + first + i, int(n), int(round(4.26 * n)), 3))
+    return [(int(n), *gen.gen_random_ksat(5000 + first + i, int(n), int(round(4.26 * n)), 3))
             for i, n in enumerate(ns)]
 
 
-def solve_config(args):
+def solve_config(args, instances=None):
     lo, hi = args.n_range
     return {"workload": f"batched solve: random 3-SAT, n ~ U[{lo},{hi}], m = round(4.26 n)",
-            "instances": args.instances, "conflict_budget": args.conflict_budget, "decisions": "VSIDS",
-            "restarts": "Luby 100",
+            "instances": instances or args.instances, "conflict_budget": args.conflict_budget,
+            "decisions": "VSIDS", "restarts": "Luby 100",
             "l2": "per-job state > L2 (one workspace slot per resident warp); no flush needed"}
 
 
-def _ref_solve_one(job):
-    """Worker: the reference's own solver (host build of its sources) on one instance."""
-    import ctypes
-    variant, n, lits, off = job
-    from oracle.ref import build_ref
-    L = ctypes.CDLL(str(build_ref.OUT / f"libref_{variant}_{__import__('platform').machine()}.so"))
-    vp = ctypes.c_void_p
-    L.ref_solve.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64, vp]
-    L.ref_solve.restype = ctypes.c_int
-    model = np.zeros(n, np.int32)
-    t0 = time.perf_counter()
-    v = L.ref_solve(lits.ctypes.data, off.ctypes.data, n, len(off) - 1, model.ctypes.data)
-    return v, time.perf_counter() - t0
+def reference_verdicts():
+    """The reference's own verdicts on instances of the solve workload, as
+    recorded in tests/golden/solve_golden.json: index -> 10 / 20, or -1 where
+    the reference did not decide within its budget."""
+    p = ROOT / "tests" / "golden" / "solve_golden.json"
+    if not p.exists():
+        return {}
+    d = json.loads(p.read_text())
+    ref = {}
+    for e in d.get("batch", []):
+        ref[int(e["index"])] = int(e["ref_nocap"]) if e["ref_nocap"] in (10, 20) else -1
+    for e in d.get("workload", {}).get("instances", []):
+        ref[int(e["index"])] = int(e["ref_nocap"]) if e["ref_nocap"] in (10, 20) else -1
+    return ref
 
 
-def ref_solve_sample(args, variant="stock"):
-    """Times the reference's solver on a bounded sample of the same instances
-    with one process per host core; instances still running at the deadline
-    count as undecided."""
-    import multiprocessing as mp
-    inst = solve_instances(args.cpu_instances, n_range=args.n_range)
-    procs = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    decided = done = 0
-    pool = ctx.Pool(procs)
+def compare_with_reference(verdicts, ref, n_range=(50, 250)):
+    """Counts of agreement between our verdicts and the reference's recorded ones."""
+    if tuple(n_range) != (50, 250):
+        return None
+    cmp_ = agree = disagree = undecided_ref = undecided_ours = 0
+    bad = []
+    for i, rv in ref.items():
+        if i >= len(verdicts):
+            continue
+        if rv < 0:
+            undecided_ref += 1
+            continue
+        v = int(verdicts[i])
+        if v == 0:
+            undecided_ours += 1
+            continue
+        cmp_ += 1
+        if v == rv:
+            agree += 1
+        else:
+            disagree += 1
+            bad.append(i)
+    return {"recorded": sum(1 for i in ref if i < len(verdicts)), "compared": cmp_, "agree": agree,
+            "disagree": disagree, "ref_undecided": undecided_ref, "unknown_here": undecided_ours,
+            "disagreeing_indices": bad[:16]}
+
+
+def host_model_check(batch, out):
+    """Every SAT verdict's model against the original clauses, on the host
+    (gpsat_check_model), independent of the device checker."""
+    import gpupsat_gb300 as g
+    ok = 0
+    sat = np.nonzero(out["verdict"] == 10)[0]
+    for f in sat:
+        lits, off = batch.formula(int(f))
+        ok += g.check_model(lits, off, batch.model_of(out, int(f)), int(batch.n_vars[f]))
+    return int(ok), int(len(sat))
+
+
+def solve_object_gpu(args, count, steps=1):
+    """The batched-solve workload on the GPU.  e2e: batch creation (host
+    preprocessing, upload) + solve + results back; value: solve calls on the
+    resident batch."""
+    import gpupsat_gb300 as g
+    inst = solve_instances(count, n_range=args.n_range)
+    formulas = [(l, o) for _, l, o in inst]
+    nv = [n for n, _, _ in inst]
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
     t0 = time.perf_counter()
-    try:
-        it = pool.imap_unordered(_ref_solve_one, [(variant, n, l, o) for n, l, o in inst])
-        while True:
-            left = args.cpu_seconds - (time.perf_counter() - t0)
-            if left <= 0:
-                break
-            try:
-                v, _ = it.next(timeout=left)
-            except StopIteration:
-                break
-            except mp.TimeoutError:
-                break
-            done += 1
-            decided += v in (10, 20)
-    finally:
-        dt = time.perf_counter() - t0
-        pool.terminate()
-    return decided / dt, decided, done, len(inst), dt, procs
+    b = g.Batch(formulas, nv)
+    out = b.solve(opts)
+    e2e_s = time.perf_counter() - t0
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = b.solve(opts)
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    v = out["verdict"]
+    decided = int((v != 0).sum())
+    st = out["stats"]
+    dev_ok = int((out["model_ok"][v == 10] == 1).sum())
+    host_ok, nsat = host_model_check(b, out)
+    if dev_ok != nsat or host_ok != nsat:
+        raise AssertionError(f"solve: {nsat} SAT verdicts, {dev_ok} models verified on the device, {host_ok} on "
+                             f"the host")
+    match = compare_with_reference(v, reference_verdicts(), args.n_range)
+    if match and match["disagree"]:
+        raise AssertionError(f"solve: verdicts differ from the reference's on instances {match['disagreeing_indices']}")
+    h2d = sum(l.nbytes + o.nbytes for l, o in formulas)
+    d2h = int(out["verdict"].nbytes + out["model"].nbytes + out["stats"].nbytes + out["model_ok"].nbytes)
+    b.close()
+    return {"metric": SOLVE_METRIC, "value": decided * steps / sum(times), "unit": "instances/s",
+            "steps": steps, "warmup": 1, "ms_per_step": 1000 * sum(times) / steps,
+            "config": solve_config(args, count),
+            "e2e": {"value": decided / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": d2h},
+            "verdicts": {"sat": int((v == 10).sum()), "unsat": int((v == 20).sum()), "unknown": int((v == 0).sum())},
+            "models_verified": {"sat": nsat, "device": dev_ok, "host": host_ok},
+            "reference_verdicts": match,
+            "conflicts": {"median": float(np.median(st[:, 0])), "mean": float(st[:, 0].mean()),
+                          "max": int(st[:, 0].max())},
+            "conflicts_per_s": float(st[:, 0].sum()) * steps / sum(times),
+            "props_per_s": float(st[:, 2].sum()) * steps / sum(times), "clocks": clk,
+            "gpu_launches": 2 * steps}
+
+
+def solve_object_ref(args):
+    """The reference's own solver (host build, iteration cap lifted) on the
+    first instances of the solve workload, one process per host core, each
+    instance with a wall budget: instances not decided within it are labelled
+    ref-undecided (their time counts).  value = decided instances / wall s."""
+    import oracle
+    from oracle.ref import pool
+    inst = solve_instances(args.cpu_instances, n_range=args.n_range, gen=oracle)
+    r = pool.solve_budgeted(inst, "nocap", budget_s=args.ref_budget, wall_s=args.cpu_seconds)
+    v = r["verdict"]
+    started = v != -2
+    decided = int(((v == 10) | (v == 20)).sum())
+    return {"metric": SOLVE_METRIC, "value": decided / r["wall"], "unit": "instances/s",
+            "config": solve_config(args, int(started.sum())),
+            "cpu_baseline": {"value": decided / r["wall"], "unit": "instances/s", "cores": r["procs"],
+                             "kind": "reference",
+                             "sample": f"first {int(started.sum())} instances of the workload started within "
+                                       f"{args.cpu_seconds:.0f} s; the reference's own solver (host build, "
+                                       f"MAX_ITERATIONS lifted), {args.ref_budget:.0f} s wall budget per instance, "
+                                       f"one process per core"},
+            "verdicts": {"sat": int((v == 10).sum()), "unsat": int((v == 20).sum()),
+                         "ref_undecided": int((v == -1).sum()), "undef": int((v == 0).sum()),
+                         "worker_died": int((v == -3).sum())},
+            "wall_s": r["wall"], "median_decided_s": float(np.median(r["seconds"][(v == 10) | (v == 20)]))
+            if decided else None}
+
+
+def latency_instances(gen=None):
+    """40 seeded uniform random 3-SAT instances, n=50, m=213 (seeds 1..40)."""
+    if gen is None:
+        import gpupsat_gb300 as gen
+    return [(s, *gen.gen_random_ksat(s, 50, 213, 3)) for s in range(1, 41)]
+
+
+def latency_object_gpu(args):
+    """One solve call per instance (a batch of one formula, resident on the
+    device), timed on the host around the call; e2e includes creating the
+    batch (preprocessing and upload)."""
+    import gpupsat_gb300 as g
+    gold = {}
+    p = ROOT / "tests" / "golden" / "solve_golden.json"
+    if p.exists():
+        gold = {e["seed"]: e["ref_nocap"] for e in json.loads(p.read_text()).get("random", [])}
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
+    call_ms, e2e_ms, agree, nsat, ok = [], [], 0, 0, 0
+    for seed, lits, off in latency_instances():
+        t0 = time.perf_counter()
+        b = g.Batch([(lits, off)], [50])
+        out = b.solve(opts)
+        e2e_ms.append(1000 * (time.perf_counter() - t0))
+        for _ in range(3):
+            t0 = time.perf_counter()
+            out = b.solve(opts)
+            call_ms.append(1000 * (time.perf_counter() - t0))
+        v = int(out["verdict"][0])
+        agree += gold.get(seed) == v
+        if v == 10:
+            nsat += 1
+            ok += int(out["model_ok"][0] == 1 and g.check_model(lits, off, b.model_of(out, 0), 50))
+        b.close()
+    return {"metric": "single-instance solve latency", "value": float(np.median(call_ms)), "unit": "ms",
+            "higher_is_better": False,
+            "config": {"workload": "single instance: random 3-SAT n=50, m=213, seeds 1..40", "calls": len(call_ms)},
+            "p90_ms": float(np.percentile(call_ms, 90)),
+            "e2e": {"value": float(np.median(e2e_ms)), "unit": "ms", "h2d_bytes_per_step": 213 * 3 * 4 + 214 * 8,
+                    "d2h_bytes_per_step": 50 + 4 + 8 * 9 + 4},
+            "verdicts_match_reference": f"{agree}/{len(gold) or 40}", "models_verified": f"{ok}/{nsat}"}
+
+
+def latency_object_ref():
+    """The reference's own solver per instance on one host core (in-process
+    calls into its host build), stock and with the iteration cap lifted."""
+    import oracle
+    res = {}
+    for variant in ("stock", "nocap"):
+        L = _ref_lib(variant)
+        ms, verd = [], []
+        for seed, lits, off in latency_instances(gen=oracle):
+            model = np.zeros(50, np.int32)
+            t0 = time.perf_counter()
+            v = L.ref_solve(lits.ctypes.data, off.ctypes.data, 50, 213, model.ctypes.data)
+            ms.append(1000 * (time.perf_counter() - t0))
+            verd.append(int(v))
+        res[variant] = {"median_ms": float(np.median(ms)), "p90_ms": float(np.percentile(ms, 90)),
+                        "decided": sum(x in (10, 20) for x in verd)}
+    return {"metric": "single-instance solve latency", "value": res["nocap"]["median_ms"], "unit": "ms",
+            "higher_is_better": False,
+            "config": {"workload": "single instance: random 3-SAT n=50, m=213, seeds 1..40", "calls": 40},
+            "cpu_baseline": {"value": res["nocap"]["median_ms"], "unit": "ms", "cores": 1, "kind": "reference",
+                             "sample": "the reference's own solver (host build), one call per instance, one core"},
+            "variants": res}
 
 
 def run_solve_reference(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    v, decided, done, total, dt, procs = ref_solve_sample(args, "stock")
-    line = {"impl": "reference", "metric": SOLVE_METRIC, "value": v, "unit": "instances/s", "n_gpus": args.gpus,
-            "steps": 1, "warmup": 0, "ms_per_step": 1000 * dt, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded uniform random 3-SAT",
-            "config": solve_config(args),
-            "cpu_baseline": {"value": v, "unit": "instances/s", "cores": procs, "kind": "reference",
-                             "sample": f"first {total} instances, {args.cpu_seconds:.0f} s wall budget: {decided} "
-                                       f"decided, {done} returned (stock MAX_ITERATIONS=1000 returns UNDEF)"},
-            "e2e": {"value": v, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    o = solve_object_ref(args)
+    line = {"impl": "reference", "metric": SOLVE_METRIC, "value": o["value"], "unit": "instances/s",
+            "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1000 * o["wall_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded uniform random 3-SAT", "config": solve_config(args),
+            "cpu_baseline": o["cpu_baseline"], "verdicts": o["verdicts"],
+            "e2e": {"value": o["value"], "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
@@ -604,55 +864,18 @@ def run_seeding_gpu(args):
 
 def run_solve_gpu(args):
     import torch
-    import gpupsat_gb300 as g
     torch.cuda.set_device(0)
-    inst = solve_instances(args.instances, n_range=args.n_range)
-    formulas = [(l, o) for _, l, o in inst]
-    nv = [n for n, _, _ in inst]
-    opts = g.solve_options(conflict_budget=args.conflict_budget)
-    b = g.Batch(formulas, nv)
-    for _ in range(args.warmup):
-        out = b.solve(opts)
-    clocks = Clocks(0)
-    torch.cuda.synchronize()
-    clocks.start()
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        out = b.solve(opts)
-        times.append(time.perf_counter() - t0)
-    clk = clocks.stop()
-    v = out["verdict"]
-    decided = int((v != 0).sum())
-    st = out["stats"]
-    value = decided * args.steps / sum(times)
-    # end to end: upload + solve + results back, from the host CNF arrays
-    e2e_t = []
-    for _ in range(max(1, min(2, args.steps))):
-        t0 = time.perf_counter()
-        bb = g.Batch(formulas, nv)
-        bb.solve(opts)
-        e2e_t.append(time.perf_counter() - t0)
-        bb.close()
-    h2d = sum(l.nbytes + o.nbytes for l, o in formulas)
-    d2h = int(out["verdict"].nbytes + out["model"].nbytes + out["stats"].nbytes + out["model_ok"].nbytes)
+    o = solve_object_gpu(args, args.instances, steps=args.steps)
     cpu = None
     if not args.no_cpu:
-        rv, rdec, rdone, rtot, rdt, procs = ref_solve_sample(args, "stock")
-        cpu = {"value": rv, "unit": "instances/s", "cores": procs, "kind": "reference",
-               "sample": f"first {rtot} instances, {args.cpu_seconds:.0f} s wall budget: {rdec} decided"}
-    line = {"metric": SOLVE_METRIC, "value": value, "unit": "instances/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded uniform random 3-SAT",
-            "config": solve_config(args), "cpu_baseline": cpu, "clocks": clk,
-            "e2e": {"value": decided * len(e2e_t) / sum(e2e_t), "unit": "instances/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": 2 * args.steps,
-            "verdicts": {"sat": int((v == 10).sum()), "unsat": int((v == 20).sum()), "unknown": int((v == 0).sum())},
-            "conflicts": {"median": float(np.median(st[:, 0])), "mean": float(st[:, 0].mean()),
-                          "max": int(st[:, 0].max())},
-            "conflicts_per_s": float(st[:, 0].sum()) * args.steps / sum(times),
-            "props_per_s": float(st[:, 2].sum()) * args.steps / sum(times)}
+        cpu = solve_object_ref(args)["cpu_baseline"]
+    line = {"metric": SOLVE_METRIC, "value": o["value"], "unit": "instances/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 1, "ms_per_step": o["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic: seeded uniform random 3-SAT",
+            "config": o["config"], "cpu_baseline": cpu, "clocks": o["clocks"], "e2e": o["e2e"],
+            "gpu_launches": o["gpu_launches"],
+            **{k: o[k] for k in ("verdicts", "models_verified", "reference_verdicts", "conflicts", "conflicts_per_s",
+                                 "props_per_s")}}
     print(json.dumps(line))
 
 
@@ -660,6 +883,8 @@ def main():
     args = parse()
     if args.instances is None:
         args.instances = {"planted": 128, "seeding": 1024}.get(args.workload, 16384)
+    if args.workload == "solve" and args.steps == 20:
+        args.steps = 1    # one batch solve is about 20 s
     if args.workload == "seeding":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned seeding; its "

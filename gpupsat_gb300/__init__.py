@@ -323,6 +323,7 @@ class BCPBatch:
     def run_device(self, trail_lits, trail_offsets, out: dict, stream: int | None = None) -> None:
         """Device buffers (torch tensors); `out` holds status, conflict, stop, n_impl, impl_lit, impl_reason, counters."""
         T = trail_offsets.numel() - 1
+        _check_device_outputs(out, T, self.impl_cap, trail_lits, trail_offsets)
         check(lib().gpsat_bcp_run_device(self._h, _p(trail_lits), _p(trail_offsets), T, _p(out["status"]),
                                          _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
                                          _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out.get("counters")),
@@ -340,6 +341,25 @@ class BCPBatch:
             pass
 
 
+def _check_device_outputs(out: dict, T: int, impl_cap: int, trail_lits, trail_offsets) -> None:
+    """The kernel writes trail t's implications at t * impl_cap: every output
+    must be a contiguous device tensor of the right dtype and shape, on the
+    trails' device, or the call is refused before it reaches the library."""
+    import torch
+    dev = trail_offsets.device
+    if trail_offsets.dtype != torch.int64 or trail_lits.dtype != torch.int32 or trail_lits.device != dev:
+        raise GpsatError(-1, "trail_lits must be int32 and trail_offsets int64, on one device")
+    want = {"status": (torch.int32, (T,)), "conflict": (torch.int32, (T,)), "stop": (torch.int32, (T,)),
+            "n_impl": (torch.int64, (T,)), "impl_lit": (torch.int32, (T, impl_cap)),
+            "impl_reason": (torch.int32, (T, impl_cap))}
+    if out.get("counters") is not None:
+        want["counters"] = (torch.int64, (T, BCP_NCOUNTERS))
+    for k, (dt, shape) in want.items():
+        a = out.get(k)
+        if a is None or a.dtype != dt or tuple(a.shape) != shape or not a.is_contiguous() or a.device != dev:
+            raise GpsatError(-1, f"out[{k!r}] must be a contiguous {dt} tensor of shape {shape} on {dev}")
+
+
 def bcp_run_static(formula: Formula, trail_lits, trail_offsets, out: dict, impl_cap: int, arena_cap: int = 0,
                    stream: int | None = None) -> None:
     """gpsat_bcp_run_static: BCP with the library's fixed device scratch (no
@@ -347,6 +367,7 @@ def bcp_run_static(formula: Formula, trail_lits, trail_offsets, out: dict, impl_
     BCPBatch.run_device; the formula must already be on the device (creating
     a BCPBatch on it uploads it)."""
     T = trail_offsets.numel() - 1
+    _check_device_outputs(out, T, impl_cap, trail_lits, trail_offsets)
     check(lib().gpsat_bcp_run_static(formula.handle, impl_cap, arena_cap, _p(trail_lits), _p(trail_offsets), T,
                                      _p(out["status"]), _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
                                      _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out.get("counters")), stream))

@@ -1175,8 +1175,8 @@ extern "C" int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, con
                                     int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,
                                     int32_t *impl_reason, int64_t *counters, void *stream)
 {
-    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index ||
-                                                !n_impl || !impl_lit || !impl_reason)))
+    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_lits || !trail_offsets || !status || !conflict_clause ||
+                                                !stop_index || !n_impl || !impl_lit || !impl_reason)))
         return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_device: bad argument");
     cudaError_t err = cudaSetDevice(b->device);
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
@@ -1385,8 +1385,8 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
                                     void *stream)
 {
     if (!f || impl_cap <= 0 || impl_cap > INT32_MAX || arena_cap < 0 || arena_cap > (1 << 24) || n_trails < 0 ||
-        (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index || !n_impl || !impl_lit ||
-                          !impl_reason)))
+        (n_trails > 0 && (!trail_lits || !trail_offsets || !status || !conflict_clause || !stop_index || !n_impl ||
+                          !impl_lit || !impl_reason)))
         return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_static: bad argument");
     if (f->h.verdict != GPSAT_UNKNOWN)
         return set_error(GPSAT_ERR_STATE, "formula was decided by preprocessing; nothing to propagate");

@@ -5,7 +5,8 @@
 // its part of gpsat_solve_options, and the device runs the chosen variant
 // inside one kernel (there are no per-operation host calls).
 //
-//   BCPStrategy        reference BCPStrategy/WatchedClausesList.cuh:33-67
+//   BCPStrategy, TrailPropagator
+//                      reference BCPStrategy/WatchedClausesList.cuh:33-67
 //   DecisionStrategy   reference SATSolver/DecisionMaker.cuh:11-29, DecisionStrategy/VSIDS.cuh
 //   ConflictAnalysis   reference ConflictAnalysis/ConflictAnalyzer.cuh:24-62
 //   ClauseLearning     reference ClauseLearning/LearntClausesManager.cuh:8-27
@@ -75,6 +76,84 @@ inline Cnf read_dimacs(const std::string &path)
     ss << in.rdbuf();
     return parse_dimacs(ss.str());
 }
+
+// A preprocessed formula held by the library (gpsat_formula).
+class Formula {
+public:
+    explicit Formula(const Cnf &f)
+    {
+        check(gpsat_formula_create(f.lits.data(), f.offsets.data(), std::max(f.n_vars, 1), f.n_clauses(), &h_),
+              "formula");
+    }
+    ~Formula() { gpsat_formula_destroy(h_); }
+    Formula(const Formula &) = delete;
+    Formula &operator=(const Formula &) = delete;
+    const gpsat_formula *get() const { return h_; }
+
+private:
+    gpsat_formula *h_ = nullptr;
+};
+
+// ---------------------------------------------------------------- BCP over trails
+// The outcome of applying one trail the way the reference applies
+// assumptions: every literal assigned, then WatchedClausesList::new_decision
+// per literal in order, depth-first over implications, until the first
+// conflict (reference BCPStrategy/WatchedClausesList.cu:46-101,
+// ConflictAnalysis/ConflictAnalyzerWithWatchedLits.cu:56-73).
+struct TrailOutcome {
+    int32_t status = GPSAT_BCP_NO_CONFLICT;  // GPSAT_BCP_*
+    int32_t conflict_clause = -1;            // preprocessed clause index
+    int32_t stop_index = -1;                 // trail position that met the conflict
+    std::vector<int32_t> implied;            // DIMACS literals, in the reference's order
+    std::vector<int32_t> reasons;            // implying clause of each
+    int64_t counters[GPSAT_BCP_NCOUNTERS] = {};
+};
+
+// The BCPStrategy role over many partial trails at once (gpsat_bcp_*): the
+// device runs each trail's propagation in the reference's order.
+class TrailPropagator {
+public:
+    TrailPropagator(const Formula &f, int64_t impl_cap, int32_t max_slots = 0, int64_t arena_cap = 0)
+        : cap_(impl_cap)
+    {
+        check(gpsat_bcp_create(f.get(), max_slots, impl_cap, arena_cap, &h_), "bcp");
+    }
+    ~TrailPropagator() { gpsat_bcp_destroy(h_); }
+    TrailPropagator(const TrailPropagator &) = delete;
+    TrailPropagator &operator=(const TrailPropagator &) = delete;
+
+    std::vector<TrailOutcome> new_decisions(const std::vector<std::vector<int32_t>> &trails)
+    {
+        const int32_t T = (int32_t)trails.size();
+        std::vector<int64_t> off(T + 1, 0);
+        for (int32_t t = 0; t < T; t++) off[t + 1] = off[t] + (int64_t)trails[t].size();
+        std::vector<int32_t> lits;
+        lits.reserve(off[T]);
+        for (const auto &tr : trails) lits.insert(lits.end(), tr.begin(), tr.end());
+        std::vector<int32_t> st(T), cc(T), si(T), il((size_t)T * cap_), ir((size_t)T * cap_);
+        std::vector<int64_t> ni(T), cn((size_t)T * GPSAT_BCP_NCOUNTERS);
+        check(gpsat_bcp_run_host(h_, lits.data(), off.data(), T, st.data(), cc.data(), si.data(), ni.data(),
+                                 il.data(), ir.data(), cn.data()),
+              "bcp run");
+        std::vector<TrailOutcome> out(T);
+        for (int32_t t = 0; t < T; t++) {
+            TrailOutcome &o = out[t];
+            o.status = st[t];
+            o.conflict_clause = cc[t];
+            o.stop_index = si[t];
+            const size_t b = (size_t)t * cap_, k = (size_t)std::max<int64_t>(0, std::min<int64_t>(ni[t], cap_));
+            o.implied.assign(il.begin() + b, il.begin() + b + k);
+            o.reasons.assign(ir.begin() + b, ir.begin() + b + k);
+            std::copy(cn.begin() + (size_t)t * GPSAT_BCP_NCOUNTERS, cn.begin() + (size_t)(t + 1) * GPSAT_BCP_NCOUNTERS,
+                      o.counters);
+        }
+        return out;
+    }
+
+private:
+    gpsat_bcp *h_ = nullptr;
+    int64_t cap_;
+};
 
 // ---------------------------------------------------------------- strategies
 struct BCPStrategy {

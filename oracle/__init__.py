@@ -6,6 +6,9 @@ library never does.
 
   bcp_ref.c   C restatement of the reference's two-watched-literal BCP in its
               own processing order (see the file header for the cited lines)
+  gen.c       the benchmark workloads' seeded generators (random k-SAT,
+              partial trails), restated so that the CPU side of the benchmark
+              never loads the shipped library; pinned to it by a CPU test
   ref/        recipe that compiles the reference's own solver sources for the
               host (output: oracle/_ref/), used to pin the restatement
 """
@@ -20,7 +23,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / f"liboracle_{platform.machine()}.so"
-SOURCES = [HERE / "bcp_ref.c"]
+SOURCES = [HERE / "bcp_ref.c", HERE / "gen.c"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -46,12 +49,34 @@ def lib() -> ctypes.CDLL:
         L.orc_bcp_destroy.argtypes = [_vp]
         L.orc_bcp_initial_watches.argtypes = [_vp, _vp, _vp]
         L.orc_bcp_run.argtypes = [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64] + [_vp] * 7
+        L.orc_gen_random_ksat.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]
+        L.orc_gen_trails.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                     ctypes.c_double, _vp, _vp]
         _lib = L
     return _lib
 
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def gen_random_ksat(seed: int, n_vars: int, n_clauses: int, k: int = 3):
+    """Uniform random k-SAT, the same instances as the library's generator. Returns (lits, offsets)."""
+    lits = np.empty(n_clauses * k, np.int32)
+    if lib().orc_gen_random_ksat(seed, n_vars, n_clauses, k, _p(lits)) != 0:
+        raise ValueError("gen_random_ksat: need 0 < k <= min(n_vars, 64)")
+    return lits, np.arange(0, n_clauses * k + 1, k, dtype=np.int64)
+
+
+def gen_trails(seed: int, n_vars: int, n_trails: int, fmin: float = 0.01, fmax: float = 0.05):
+    """Random partial trails, the same as the library's generator. Returns (lits, offsets)."""
+    off = np.empty(n_trails + 1, np.int64)
+    if lib().orc_gen_trails(seed, n_vars, n_trails, fmin, fmax, _p(off), None) != 0:
+        raise ValueError("gen_trails: need n_vars > 0, 0 <= fmin <= fmax <= 1")
+    lits = np.empty(int(off[-1]), np.int32)
+    if lib().orc_gen_trails(seed, n_vars, n_trails, fmin, fmax, _p(off), _p(lits)) != 0:
+        raise MemoryError("gen_trails")
+    return lits, off
 
 
 class BCPOracle:

@@ -20,9 +20,10 @@ Recipe (nothing in the reference tree is modified):
      and Preprocessing units (the device branches are the implemented ones);
   3. link them with oracle/ref/ref_driver.cpp into a shared library.
 
-The reference is found at $GPSAT_REFERENCE or /root/reference.  Where it is
-absent (the GPU machine), an existing build-dir copy under oracle/_ref/ is
-compiled instead; with neither, build() reports that it cannot build.
+The reference checkout is named by $GPSAT_REFERENCE (the directory that holds
+its src/).  Without it (as on the GPU machine), an existing build-dir copy under
+oracle/_ref/ is compiled instead; with neither, build() raises
+FileNotFoundError saying so.
 It needs Boost for nothing: the CLI/parser units that use Boost are skipped.
 """
 from __future__ import annotations
@@ -52,15 +53,19 @@ UNITS = [
     "Preprocessing/RepeatedLiteralsRemover.cu", "Preprocessing/UnaryClausesRemover.cu",
     "Restarts/GeometricRestartsManager.cu", "SATSolver/Backtracker.cu", "SATSolver/DecisionMaker.cu",
     "SATSolver/SATSolver.cu", "SATSolver/SolverTypes.cu", "SATSolver/VariablesStateHandler.cu",
-    "Statistics/RuntimeStatistics.cu", "Utils/CUDAClauseVec.cu",
+    "Statistics/RuntimeStatistics.cu", "Utils/CUDAClauseVec.cu", "JobsManager/VariableChooser.cu",
 ]
 HOST_SIDE = {"Utils/CUDAClauseVec.cu", "FileManager/FormulaData.cu", "Preprocessing/RepeatedLiteralsRemover.cu",
-             "Preprocessing/UnaryClausesRemover.cu"}
+             "Preprocessing/UnaryClausesRemover.cu", "JobsManager/VariableChooser.cu"}
 VARIANTS = {"stock": None, "nocap": ("#define MAX_ITERATIONS 1000", "#define MAX_ITERATIONS 2000000000")}
 
 
 def reference_src() -> Path | None:
-    cand = Path(os.environ.get("GPSAT_REFERENCE", "/root/reference")) / "src"
+    """src/ of the checkout named by $GPSAT_REFERENCE, or None."""
+    root = os.environ.get("GPSAT_REFERENCE")
+    if not root:
+        return None
+    cand = Path(root) / "src"
     return cand if (cand / "SATSolver" / "SATSolver.cu").exists() else None
 
 
@@ -76,7 +81,8 @@ def _prepare_copy(variant: str) -> Path:
     ref = reference_src()
     if ref is None:
         if not (dst / "SATSolver" / "SATSolver.cu").exists():
-            raise FileNotFoundError("reference sources not found and no build-dir copy present")
+            raise FileNotFoundError("no build-dir copy of the reference under oracle/_ref and $GPSAT_REFERENCE "
+                                    "does not name a reference checkout (the directory holding src/)")
         return dst
     stamp = dst / ".copied"
     if stamp.exists():
@@ -103,7 +109,7 @@ def _compile(args):
 
 def build_variant(variant: str) -> Path:
     lib = OUT / f"libref_{variant}_{platform.machine()}.so"
-    if lib.exists():
+    if lib.exists() and lib.stat().st_mtime >= DRIVER.stat().st_mtime:
         return lib
     src = _prepare_copy(variant)
     obj = OUT / f"obj_{variant}_{platform.machine()}"
@@ -116,6 +122,8 @@ def build_variant(variant: str) -> Path:
         extra = [] if u in HOST_SIDE else ["-D__CUDA_ARCH__=900"]
         jobs.append((base + extra + ["-c", str(src / u), "-o", str(o)], o))
     drv = obj / "ref_driver.o"
+    if drv.exists() and drv.stat().st_mtime < DRIVER.stat().st_mtime:
+        drv.unlink()
     jobs.append((base + ["-D__CUDA_ARCH__=900", "-c", str(DRIVER), "-o", str(drv)], drv))
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(_compile, jobs))

@@ -17,12 +17,14 @@
  * WatchedClausesList::new_decision per literal with one shared pending list,
  * stopping at the first conflict (ConflictAnalysis/ConflictAnalyzerWithWatchedLits.cu:56-73).
  */
+#include <chrono>
 #include <cstdint>
 #include <unordered_map>
 #include <vector>
 
 #include "BCPStrategy/WatchedClausesList.cuh"
 #include "FileManager/FormulaData.cuh"
+#include "JobsManager/VariableChooser.cuh"
 #include "SATSolver/SATSolver.cuh"
 #include "SATSolver/VariablesStateHandler.cuh"
 #include "Statistics/RuntimeStatistics.cuh"
@@ -99,11 +101,26 @@ int ref_solve(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n
     return verdict;
 }
 
+int ref_bcp_timed(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_clauses, const int32_t *trail,
+                  int64_t trail_len, int64_t cap, int32_t *impl_lit, int32_t *impl_reason, int64_t *n_impl,
+                  int32_t *conflict_clause, int32_t *stop_index, double *seconds);
+
 /* Returns 0 (no conflict), 1 (conflict), -2 (a variable given both signs),
  * -3 (preprocessing decided the formula), -1 (implication capacity). */
 int ref_bcp(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_clauses, const int32_t *trail,
             int64_t trail_len, int64_t cap, int32_t *impl_lit, int32_t *impl_reason, int64_t *n_impl,
             int32_t *conflict_clause, int32_t *stop_index)
+{
+    return ref_bcp_timed(lits, off, n_vars, n_clauses, trail, trail_len, cap, impl_lit, impl_reason, n_impl,
+                         conflict_clause, stop_index, nullptr);
+}
+
+/* ref_bcp, and with seconds != NULL the wall time of the trail application
+ * alone (the assignments and the new_decision calls), without the set-up of
+ * the formula and the watch lists that precedes it. */
+int ref_bcp_timed(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_clauses, const int32_t *trail,
+                  int64_t trail_len, int64_t cap, int32_t *impl_lit, int32_t *impl_reason, int64_t *n_impl,
+                  int32_t *conflict_clause, int32_t *stop_index, double *seconds)
 {
     *n_impl = 0;
     *conflict_clause = -1;
@@ -123,6 +140,7 @@ int ref_bcp(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_c
     auto *wcl = new WatchedClausesList(n_vars, handler, repo, formula.size_of());
     wcl->add_all_clauses(formula);
     handler->set_decision_level(1);
+    const auto t0 = std::chrono::steady_clock::now();
     std::vector<Decision> ds;
     for (int64_t i = 0; i < trail_len; i++) {
         int32_t d = trail[i];
@@ -147,6 +165,7 @@ int ref_bcp(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_c
             break;
         }
     }
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     auto it = pending.get_iterator();
     int64_t k = 0;
     while (it.has_next()) {
@@ -159,6 +178,31 @@ int ref_bcp(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_c
     }
     *n_impl = k;
     return rc;
+}
+
+/* The reference's split-variable ranking: VariableChooser::evaluate over the
+ * preprocessed clauses, as MaxClauseJobChooser uses it (SATSolver/main.cu:221,
+ * JobsManager/VariableChooser.cu:23-40).  order[i] = 1-based variable at rank
+ * i, score[i] its evaluation; returns the number of ranked variables. */
+int ref_rank_vars(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_clauses, int32_t *order,
+                  int32_t *score)
+{
+    FormulaData *fd = make_formula(lits, off, n_vars, n_clauses);
+    std::vector<Clause> const &formula = *fd->get_formula_host();
+    VariableChooser vc(formula, (size_t)n_vars);
+    vc.evaluate();
+    // the evaluation of each variable, recomputed the way evaluate() sums it
+    std::vector<int32_t> ev(n_vars, 0);
+    for (Clause const &c : formula)
+        for (size_t j = 0; j < c.n_lits; j++) ev[var(c.literals[j])] += var(c.literals[j]);
+    int32_t k = 0;
+    while (vc.has_next_var() && k < n_vars) {
+        Var v = vc.next_var();
+        order[k] = (int32_t)v + 1;
+        score[k] = ev[v];
+        k++;
+    }
+    return k;
 }
 
 /* Clauses after the reference's preprocessing and its initial watches. */

@@ -1,9 +1,10 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference sources (it builds the host copy of
-the reference with oracle/ref/build_ref.py first):
+Run in a container that has the reference sources, named by $GPSAT_REFERENCE
+(it builds the host copy of the reference with oracle/ref/build_ref.py first):
 
-    python tests/golden/make_golden.py
+    GPSAT_REFERENCE=<reference checkout> python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --workload-only   # only the workload sample
 
 Outputs (committed):
   bcp_golden.npz     formulas + trails + the reference BCP's outputs
@@ -15,7 +16,10 @@ Outputs (committed):
   solve_golden.json  the reference's six CNF fixtures (tests/cnf/*.cnf, with
                      their .expected verdicts) plus seeded random 3-SAT at
                      n=50 and the verdicts of the reference's sequential solver
-                     (stock iteration cap and lifted cap)
+                     (stock iteration cap and lifted cap), the reference's
+                     verdicts on n <= 150 instances of the batched-solve
+                     workload ("batch"), and on its first 512 instances with a
+                     wall budget per instance ("workload")
 Inputs are seeded; the generator is the library's own (splitmix64 streams).
 """
 from __future__ import annotations
@@ -215,9 +219,35 @@ def batch_cases():
     print("batch sample:", len(out), "decided by the reference:", sum(o["ref_nocap"] in (10, 20) for o in out))
 
 
+def workload_cases(count=512, budget_s=30.0):
+    """The reference's verdicts (iteration cap lifted) on the first `count`
+    instances of the batched-solve workload (n ~ U[50, 250], ratio 4.26:
+    instance i has n = default_rng(11).integers(50, 251, 16384)[i] and formula
+    seed 5000 + i), each with a wall budget of budget_s seconds on one host
+    core; an instance not decided within it is recorded as ref-undecided (-1)."""
+    from oracle.ref import pool
+    ns = np.random.default_rng(11).integers(50, 251, size=16384)[:count]
+    inst = []
+    for i, n in enumerate(ns):
+        lits, off = g.gen_random_ksat(5000 + i, int(n), int(round(4.26 * n)), 3)
+        inst.append((int(n), lits, off))
+    r = pool.solve_budgeted(inst, "nocap", budget_s=budget_s)
+    out = [dict(index=i, seed=5000 + i, n=int(ns[i]), ref_nocap=int(r["verdict"][i]),
+                seconds=round(float(r["seconds"][i]), 3)) for i in range(count)]
+    data = json.loads((OUT / "solve_golden.json").read_text())
+    data["workload"] = dict(budget_s=budget_s, procs=r["procs"], instances=out)
+    (OUT / "solve_golden.json").write_text(json.dumps(data, indent=1))
+    dec = sum(o["ref_nocap"] in (10, 20) for o in out)
+    print(f"workload sample: {count} instances, {dec} decided by the reference within {budget_s} s each")
+
+
 if __name__ == "__main__":
+    if "--workload-only" in sys.argv:
+        workload_cases()
+        sys.exit(0)
     stock, nocap = load("stock"), load("nocap")
     bcp_cases(stock)
     preprocess_cases(stock)
     solve_cases(stock, nocap)
     batch_cases()
+    workload_cases()

@@ -77,10 +77,12 @@ def test_static_entry_rejects_state_beyond_its_scratch(gpsat, cuda_ok):
     gpsat.BCPBatch(f, impl_cap=64)
     tl, to = gpsat.gen_trails(52, n, 4, 0.01, 0.05)
     d_tl, d_to = torch.from_numpy(tl).to(dev), torch.from_numpy(to).to(dev)
-    big = 9 << 20                                    # 72 MiB of stack for one trail
+    # 2^24 watch moves of room for one trail is far beyond the 64 MiB array;
+    # the output buffers match impl_cap, so even a call that got through
+    # would stay inside them
     out = device_out(torch, 4, 1, dev)
     with pytest.raises(gpsat.GpsatError) as e:
-        gpsat.bcp_run_static(f, d_tl, d_to, out, impl_cap=big)
+        gpsat.bcp_run_static(f, d_tl, d_to, out, impl_cap=1, arena_cap=1 << 24)
     assert e.value.code == -6 and "static scratch holds 67108864 bytes" in str(e.value)  # GPSAT_ERR_CAPACITY
     torch.cuda.synchronize()
     assert (out["status"] == -7).all()                # nothing was launched
