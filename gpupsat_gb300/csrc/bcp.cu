@@ -18,15 +18,19 @@
 //     w0ent[]  32 bytes per initial watch: {clause, literal offset, length,
 //              (w1<<16)|w2} {first four literals}; each var's entries in the
 //              reference's initial list order
-//   per trail slot (one warp owns one slot; slots are reused across trails)
-//     vr[n]     8 bytes per var: dh  uint32 (epoch<<24)|arena index, head of the
-//               clauses add_first'ed to the var; asg uint8 (epoch<<1)|sign, trail
-//               + pending implications (one load reads both)
-//     cst[m]    uint32 (epoch<<24)|(blocked<<22)|(w1<<11)|w2   clauses touched
-//     arena[]   32 bytes per entry: {clause, literal offset, length, next} {literals}
-//     stack[]   int2 depth-first frames (intervals of the implication list)
-//   A slot's epoch (1..127) advances per trail, so nothing is cleared between
-//   trails; the slot is wiped once every 127 trails.
+//   per trail slot (one thread block owns one slot; slots are reused)
+//     asg[n/16]  2 bits per variable (assigned, sign): the trail literals and
+//                the pending implications; zero between trails (a trail
+//                clears the words it set)
+//     dh[n]      uint32 (epoch<<24)|arena index: head of the clauses
+//                add_first'ed to the variable
+//     cst[m]     uint32 (epoch<<24)|(blocked<<22)|(w1<<11)|w2: clauses whose
+//                watches moved or that were blocked
+//     arena[]    32 bytes per entry: {clause, literal offset, length, next} {literals}
+//     stack[]    int2 depth-first frames (intervals of the implication list)
+//     impl[]     the implied literals (internal encoding), read by the descent
+//   A slot's epoch (1..255) advances per trail, so dh and cst are not cleared
+//   between trails; the slot wipes them once every 255 trails.
 //
 // Current list of var v = clauses add_first'ed to v (newest first) followed by
 // v's initial list, keeping entries whose clause still watches v and is not
@@ -34,20 +38,26 @@
 // false literals and nothing is unassigned within one BCP), so that is the
 // reference's linked list exactly.
 //
-// Execution: one warp per trail.  A round gathers up to 32 upcoming watch
-// entries -- the rest of the current scan and, while the current scan is a
-// trail scan that has implied nothing, the entries of the following trail
-// scans -- and evaluates all of them at once against the current state, with
-// every random load of the round (clause state, assignments, list heads) in
-// one trip.  It then commits them in reference order up to the first event
-// that could have changed a later evaluation: an entry whose clause an earlier
-// entry of the round already handled, a later scan whose list is not what the
-// round assumed (it has clauses add_first'ed to it, possibly by this round),
-// the entry just after a conflict, the end of the scan an implication was
-// found in (its depth-first descent comes first), or a later entry of that
-// scan whose clause has the implied variable.  Events are encoded as ordered
-// keys and the cut is one warp min-reduction.  Uncommitted entries are
-// evaluated again next round, so the result is the sequential one.
+// Execution: one thread block (NW warps) per trail.  A round lays out a window
+// of up to 32*NW upcoming watch entries -- the rest of the current scan and,
+// while the current scan is a trail scan that has implied nothing, the entries
+// of up to 31 following trail scans -- and thread p evaluates window position
+// p against the round-start state, with every random load of the round in one
+// trip.  The round then commits the entries in reference order up to the first
+// event that could have changed a later evaluation (an entry whose clause an
+// earlier window scan holds, a later scan whose list is not what the round
+// assumed or gets a clause moved into it, the entry just after a conflict, the
+// end of the scan an implication was found in -- its depth-first descent comes
+// first -- and a later entry of that scan whose clause has the implied
+// variable).  Events are ordered integer keys and the cut is one block-wide
+// minimum.  Uncommitted entries are evaluated again next round, so the result
+// is the sequential one.
+//
+// The following scans come from a look-ahead ring of upcoming trail positions
+// (variable, initial-list range, and the list head as loaded when the position
+// entered the ring), filled two rounds ahead by warp 1.  A head loaded then may
+// be stale; every window scan's head is loaded again in the round's entry trip
+// and a scan whose list changed is cut from the window.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -62,21 +72,24 @@ namespace gpsat {
 namespace bcp {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int WARPS = 4;          // warps per block
 constexpr int KIN = 4;            // clause literals stored inside a watch entry
-constexpr uint32_t EPMAX = 127;   // epochs per slot before a wipe
+constexpr uint32_t EPMAX = 255;   // epochs per slot before a wipe
 constexpr int MAXLEN = 2048;      // clause length limit (11-bit watch indices)
+constexpr int MAXSC = 32;         // window scans (the current one + 31 following)
+constexpr int LB = 128;           // look-ahead ring positions
+constexpr int CHUNK = 32;         // ring refill granularity (one warp)
+constexpr int LEAD = 96;          // ring positions kept ahead of the trail cursor
 constexpr int64_t MAX_ITERS = int64_t(1) << 26;  // per-trail loop iterations before GPSAT_BCP_BUDGET
 
-enum : int { A_NONE = 0, A_SW1 = 1, A_SW2 = 2, A_BLOCK = 3, A_IMPLY = 4, A_CONFLICT = 5 };
+#ifndef GPSAT_BCP_WARPS
+#define GPSAT_BCP_WARPS 4
+#endif
+constexpr int NW = GPSAT_BCP_WARPS;   // warps per block: one trail per block
+constexpr int NT = NW * 32;
+constexpr int W = NT;                 // window entries: one per thread
+static_assert(NW >= 2 && W <= 256 && LB >= LEAD + CHUNK, "layout limits");
 
-// per-variable record of a trail slot
-struct VarRec {
-    uint32_t dh;       // (epoch<<24)|arena index: head of the clauses add_first'ed to the var
-    uint8_t asg;       // (epoch<<1)|sign: trail literal or pending implication
-    uint8_t pad[3];
-};
-static_assert(sizeof(VarRec) == 8 && offsetof(VarRec, asg) == 4, "the assignment byte starts a 4-byte word");
+enum : int { A_NONE = 0, A_SW1 = 1, A_SW2 = 2, A_BLOCK = 3, A_IMPLY = 4, A_CONFLICT = 5 };
 
 struct Dev {
     int32_t n_vars;
@@ -84,14 +97,16 @@ struct Dev {
     const int32_t *__restrict__ lits;
     const uint32_t *__restrict__ w0off;
     const int4 *__restrict__ w0ent;   // 2 int4 per entry
-    VarRec *vr;
+    uint32_t *asg;
+    uint32_t *dh;
     uint32_t *cst;
     int4 *arena;                      // 2 int4 per entry
     int2 *stack;
+    int32_t *impl;
     uint32_t *epoch;
     unsigned int *next_trail;
     const int32_t *order;             // trails in processing order (null: index order)
-    int64_t n_pad, m_pad, arena_cap, impl_cap;
+    int64_t n_words, n_pad, m_pad, arena_cap, impl_cap;
     int32_t n_slots;
     const int32_t *__restrict__ trail;
     const int64_t *__restrict__ toff;
@@ -102,28 +117,43 @@ struct Dev {
     int64_t *counters;
 };
 
-struct WarpSmem {
-    int4 e0[32];
-    int4 e1[32];
-    int32_t dp_after[32];
-    int32_t sc_var[33];
-    int32_t sc_begin[33];
-    int32_t sc_end[33];
-    uint32_t sc_wk[33];
-    uint32_t sc_wend[33];
-    uint8_t q2j[1024];      // look-ahead buffer: entry stream offset -> buffer position
+struct Smem {
+    // window layout (written by warp 0 / thread 0, read by all)
+    int sc_var[MAXSC];
+    int sc_b[MAXSC];
+    int sc_e[MAXSC];
+    uint32_t sc_wk[MAXSC];
+    uint32_t sc_wend[MAXSC];
+    int32_t sc_head[MAXSC];    // following scan: arena index of the assumed added head, or -1
+    uint32_t sc_h[MAXSC];      // following scan: the list-head word the layout assumed
+    int32_t sc_next[MAXSC];    // following scan: what comes after its added head (-1: nothing)
+    uint8_t pos_scan[W];
+    int4 dyn0[W];              // the current scan's added entries (thread 0 follows the chain)
+    int4 dyn1[W];
+    int32_t dyn_next[W];
+    int ndyn, dyn_done, nsc, nent;
+    // events of the round
+    int key_min;
+    int imp_cnt;
+    int16_t imp_pos[W];
+    int8_t imp_scan[W];
+    int32_t imp_var[W];
+    int wcnt_im[NW], wcnt_mv[NW];
+    int32_t mh[2 * W];         // move targets of the round (collision check)
+    int collide;
+    int32_t mv_t1[W], mv_t2[W];
+    int32_t confl_c, confl_scan;
+    unsigned long long red[NW][3];
+    int t;
+    // look-ahead ring: trail position q lives in slot q % LB
+    int32_t lb_var[LB];
+    uint32_t lb_a[LB], lb_b[LB], lb_h[LB];
 };
 
 __device__ __forceinline__ unsigned lanemask_lt()
 {
     unsigned r;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ unsigned lanemask_gt()
-{
-    unsigned r;
-    asm("mov.u32 %0, %%lanemask_gt;" : "=r"(r));
     return r;
 }
 template <class T>
@@ -135,54 +165,36 @@ __device__ __forceinline__ T warp_sum(T x)
 }
 __device__ __forceinline__ int32_t dimacs_of(int32_t l) { return (l & 1) ? (l >> 1) + 1 : -((l >> 1) + 1); }
 
-// position of the n-th set bit of m (n >= 1, m holds at least n set bits)
-__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
-{
-    int pos = 0;
-#pragma unroll
-    for (int w = 16; w >= 1; w >>= 1) {
-        const int c = __popc(m & ((1u << w) - 1u));
-        if (c < n) {
-            n -= c;
-            m >>= w;
-            pos += w;
-        }
-    }
-    return pos;
-}
-
-// literal l is consistent (unassigned in this epoch, or true) given its var's asg byte
-__device__ __forceinline__ bool cons_of(uint8_t a, int32_t l, uint32_t e)
-{
-    return ((uint32_t)(a >> 1) != e) || ((a & 1) == (l & 1));
-}
+// assignment bits of variable v inside its word: bit 0 assigned, bit 1 sign (1 = true)
+__device__ __forceinline__ uint32_t asg_bits(uint32_t word, int32_t v) { return (word >> ((v & 15) << 1)) & 3u; }
+// literal l is consistent (unassigned, or true) given its variable's bits
+__device__ __forceinline__ bool cons_of(uint32_t b, int32_t l) { return !(b & 1u) || ((b >> 1) == (uint32_t)(l & 1)); }
 
 struct Eval {
     int act;
     int nw1, nw2;       // new watch indices (switch)
     int32_t t1, t2;     // switch target vars
-    uint32_t dh1, dh2;  // their list heads as loaded
     int32_t unit;       // unit literal (imply)
     int acnt;           // assignment lookups as the reference counts them
 };
 
 // process_clause of the reference for a clause too long for the inline path
-// (literals read from the arena).
-__device__ __noinline__ void eval_long(const Dev &d, const VarRec *vr, int off, int len,
-                                       int w1, int w2, uint32_t e, Eval &r)
+// (literals and their assignment words read from memory one by one).
+__device__ __noinline__ void eval_long(const Dev &d, const uint32_t *asg, int off, int len, int w1, int w2, Eval &r)
 {
     const int32_t *L = d.lits + off;
-    int32_t l1 = L[w1], l2 = L[w2];
-    bool c1 = cons_of(vr[l1 >> 1].asg, l1, e), c2 = cons_of(vr[l2 >> 1].asg, l2, e);
+    const int32_t l1 = L[w1], l2 = L[w2];
+    const bool c1 = cons_of(asg_bits(asg[(l1 >> 1) >> 4], l1 >> 1), l1);
+    const bool c2 = cons_of(asg_bits(asg[(l2 >> 1) >> 4], l2 >> 1), l2);
     r.acnt = 2;
     r.act = A_NONE;
     if (c1 && c2) return;
     int pend = (!c1 && !c2) ? 2 : 1, f1 = -1, f2 = -1;
     for (int i = 0; pend > 0 && i < len; i++) {
         if (i == w1 || i == w2) continue;
-        int32_t l = L[i];
+        const int32_t l = L[i];
         r.acnt++;
-        if (cons_of(vr[l >> 1].asg, l, e)) {
+        if (cons_of(asg_bits(asg[(l >> 1) >> 4], l >> 1), l)) {
             if (f1 < 0) f1 = i;
             else f2 = i;
             pend--;
@@ -197,7 +209,6 @@ __device__ __noinline__ void eval_long(const Dev &d, const VarRec *vr, int off, 
             r.nw1 = c1 ? w1 : f1;
             r.nw2 = c1 ? f1 : w2;
             r.t1 = L[f1] >> 1;
-            r.dh1 = vr[r.t1].dh;
             return;
         }
     } else if (f1 >= 0 && f2 >= 0) {
@@ -206,8 +217,6 @@ __device__ __noinline__ void eval_long(const Dev &d, const VarRec *vr, int off, 
         r.nw2 = f2;
         r.t1 = L[f1] >> 1;
         r.t2 = L[f2] >> 1;
-        r.dh1 = vr[r.t1].dh;
-        r.dh2 = vr[r.t2].dh;
         return;
     } else if (f1 >= 0) {
         unit = L[f1];
@@ -216,81 +225,118 @@ __device__ __noinline__ void eval_long(const Dev &d, const VarRec *vr, int off, 
         return;
     }
     r.unit = unit;
-    r.act = ((uint32_t)(vr[unit >> 1].asg >> 1) != e) ? A_IMPLY : A_BLOCK;
+    r.act = (asg_bits(asg[(unit >> 1) >> 4], unit >> 1) & 1u) ? A_BLOCK : A_IMPLY;
 }
 
-// commit-cut keys: (lane position << 7) | (window scan << 1) | after
+// commit-cut keys: (window position << 7) | (window scan << 1) | after
 constexpr int NO_CUT = INT_MAX;
 __device__ __forceinline__ int key_before(int pos, int scan) { return (pos << 7) | (scan << 1); }
 __device__ __forceinline__ int key_after(int pos, int scan) { return ((pos + 1) << 7) | (scan << 1) | 1; }
 
-__device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int lane)
+// block-wide minimum; every thread gets it
+__device__ __forceinline__ int block_min(Smem &sm, int v)
 {
-    VarRec *vr = d.vr + (size_t)slot * d.n_pad;
+    v = __reduce_min_sync(FULL, v);
+    if ((threadIdx.x & 31) == 0) atomicMin(&sm.key_min, v);
+    __syncthreads();
+    return sm.key_min;
+}
+
+// The ring chunk that warp 1 carries between rounds: lanes hold trail
+// positions [ring_hi + 32, +32) as literals (stage 1) and [ring_hi, +32) as
+// variable, initial-list range and list head in flight (stage 2).
+struct RingPipe {
+    int32_t lit;
+    int32_t var;
+    uint32_t a, b, h;
+};
+
+__device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slot)
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t *asg = d.asg + (size_t)slot * d.n_words;
+    uint32_t *dh = d.dh + (size_t)slot * d.n_pad;
     uint32_t *cst = d.cst + (size_t)slot * d.m_pad;
     int4 *arena = d.arena + (size_t)slot * d.arena_cap * 2;
     int2 *stk = d.stack + (size_t)slot * d.impl_cap;
+    int32_t *impl = d.impl + (size_t)slot * d.impl_cap;
     int32_t *ilit = d.ilit + (size_t)t * d.impl_cap;
     int32_t *ireason = d.ireason + (size_t)t * d.impl_cap;
     const int32_t n = d.n_vars;
     const unsigned lt = lanemask_lt();
 
     // ---- epoch of this slot
-    uint32_t e = 0;
-    if (lane == 0) e = d.epoch[slot] + 1;
-    e = __shfl_sync(FULL, e, 0);
+    uint32_t e = d.epoch[slot] + 1;
     if (e > EPMAX) {
-        uint4 z = make_uint4(0, 0, 0, 0);
-        uint4 *v4 = reinterpret_cast<uint4 *>(vr);
-        for (int64_t i = lane; i < d.n_pad / 2; i += 32) v4[i] = z;
+        const uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dh);
+        for (int64_t i = tid; i < d.n_pad / 4; i += NT) d4[i] = z;
         uint4 *c4 = reinterpret_cast<uint4 *>(cst);
-        for (int64_t i = lane; i < d.m_pad / 4; i += 32) c4[i] = z;
+        for (int64_t i = tid; i < d.m_pad / 4; i += NT) c4[i] = z;
         e = 1;
-        __syncwarp();
     }
-    if (lane == 0) d.epoch[slot] = e;
-
     const int64_t tb = d.toff[t];
     const int64_t tn = d.toff[t + 1] - tb;
+    __syncthreads();
+    if (tid == 0) d.epoch[slot] = e;
 
-    // ---- assign every trail literal first, in one pass: an exchange on the
-    // word that holds the assignment byte (the rest of the word is padding)
-    // returns what was there, and the same variable given the other sign
-    // earlier in this trail (by any lane) shows as this epoch's opposite sign
+    // ---- assign every trail literal first: an atomic OR of its two bits; the
+    // old word shows the variable assigned the other way earlier (by any thread)
     bool bad = tn < 0;
-    // (unrolled so that several iterations' loads are in flight at once)
 #pragma unroll 4
-    for (int64_t i = lane; i < tn; i += 32) {
+    for (int64_t i = tid; i < tn; i += NT) {
         const int32_t x = d.trail[tb + i];
         if (x == 0 || x > n || x < -n) {
             bad = true;
         } else {
-            const unsigned a = (e << 1) | (x > 0 ? 1u : 0u);
-            const unsigned old = atomicExch(reinterpret_cast<unsigned *>(&vr[(x > 0 ? x : -x) - 1].asg), a) & 0xFFu;
-            if ((old >> 1) == e && old != a) bad = true;
+            const int32_t v = (x > 0 ? x : -x) - 1;
+            const int sh = (v & 15) << 1;
+            const uint32_t bits = (x > 0 ? 3u : 1u) << sh;
+            const uint32_t old = atomicOr(&asg[v >> 4], bits);
+            if (((old >> sh) & 1u) && (((old ^ bits) >> sh) & 2u)) bad = true;
         }
     }
-    bad = __any_sync(FULL, bad);
-    __syncwarp();
+
+    // ---- fill the look-ahead ring with the first LEAD positions, and start
+    // the pipelined refill after them
+    RingPipe pipe;
+    pipe.lit = pipe.var = 0;
+    pipe.a = pipe.b = pipe.h = 0;
+    int64_t ring_hi = tn < LEAD ? (tn > 0 ? tn : 0) : LEAD;   // positions [0, ring_hi) are in the ring
+    for (int64_t q = tid; q < ring_hi; q += NT) {
+        const int32_t x = d.trail[tb + q];
+        int32_t v = (x > 0 ? x : -x) - 1;
+        if (v < 0 || v >= n) v = 0;   // a bad trail never reads the ring
+        const int r = (int)(q & (LB - 1));
+        sm.lb_var[r] = v;
+        sm.lb_a[r] = d.w0off[v];
+        sm.lb_b[r] = d.w0off[v + 1];
+        sm.lb_h[r] = dh[v];
+    }
+    if (wid == 1 && ring_hi < tn) {
+        const int64_t q = ring_hi + lane;
+        if (q < tn) {
+            const int32_t x = d.trail[tb + q];
+            int32_t v = (x > 0 ? x : -x) - 1;
+            if (v < 0 || v >= n) v = 0;
+            pipe.var = v;
+            pipe.a = d.w0off[v];
+            pipe.b = d.w0off[v + 1];
+            pipe.h = dh[v];
+        }
+        const int64_t q2 = ring_hi + CHUNK + lane;
+        if (q2 < tn) pipe.lit = d.trail[tb + q2];
+    }
+    bad = __syncthreads_or(bad);
 
     int64_t n_impl = 0, props = 0, cI = 0;
-    int64_t myW = 0, myL = 0, myA = 0;  // lane-private, reduced at the end
+    int64_t myW = 0, myL = 0, myA = 0;  // thread-private, reduced at the end
     int32_t status = bad ? GPSAT_BCP_BAD_TRAIL : GPSAT_BCP_NO_CONFLICT, confl = -1, stopi = -1;
     int64_t arena_used = 0, ti = 0, top_j = 0, top_e = 0, cur_impl_start = 0, cur_trail = -1, dfs_trail = -1;
     int depth = 0;
     bool in_scan = false, cur_counted = false, cur_is_trail = false;
     int32_t cur_var = 0, cur_dp = -1;
     uint32_t cur_wk = 0, cur_wend = 0;
-    // look-ahead buffer: lane j holds trail position lb_base + j (its variable
-    // and initial watch-list range; positions past the trail: empty).  When
-    // fewer than 16 lie ahead it advances by 16 from values loaded one advance
-    // earlier: lanes 0-15 of nx_* hold positions lb_base + 32.. (their list
-    // ranges in flight) and nnx the trail literals of lb_base + 48.., so an
-    // advance waits on no load.
-    int64_t lb_base = INT64_MIN / 2;
-    int32_t lb_v = 0, nx_v = 0, nnx = 0;
-    uint32_t lb_a = 0, lb_b = 0, nx_a = 0, nx_b = 0;
-    int lb_p = 0;
     // every iteration finishes a scan, pops a frame or commits at least one
     // entry; the budget only guarantees termination if that were ever broken
     int64_t budget = MAX_ITERS;
@@ -305,15 +351,16 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             int32_t v;
             if (depth > 0) {
                 if (top_j < top_e) {
-                    int32_t x = ilit[top_j];
+                    v = impl[top_j] >> 1;
                     top_j++;
-                    v = (x > 0 ? x : -x) - 1;
                     cur_is_trail = false;
                     cur_trail = dfs_trail;
+                    cur_wk = d.w0off[v];
+                    cur_wend = d.w0off[v + 1];
                 } else {
                     depth--;
                     if (depth > 0) {
-                        int2 fr = stk[depth - 1];
+                        const int2 fr = stk[depth - 1];
                         top_j = fr.x;
                         top_e = fr.y;
                     }
@@ -321,33 +368,25 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 }
             } else {
                 if (ti >= tn) break;
-                v = -1;
-                const int64_t bo = ti - lb_base;
-                if (bo >= 0 && bo < 32) {
-                    // the look-ahead buffer holds this position's variable and range
-                    v = __shfl_sync(FULL, lb_v, (int)bo);
-                    cur_wk = __shfl_sync(FULL, lb_a, (int)bo);
-                    cur_wend = __shfl_sync(FULL, lb_b, (int)bo);
+                if (ti < ring_hi) {
+                    const int r = (int)(ti & (LB - 1));
+                    v = sm.lb_var[r];
+                    cur_wk = sm.lb_a[r];
+                    cur_wend = sm.lb_b[r];
                 } else {
-                    int32_t x = d.trail[tb + ti];
+                    const int32_t x = d.trail[tb + ti];
                     v = (x > 0 ? x : -x) - 1;
+                    cur_wk = d.w0off[v];
+                    cur_wend = d.w0off[v + 1];
                 }
                 cur_trail = ti;
                 dfs_trail = ti;
                 ti++;
                 cur_is_trail = true;
-                if (bo < 0 || bo >= 32) {
-                    cur_wk = d.w0off[v];
-                    cur_wend = d.w0off[v + 1];
-                }
             }
-            uint32_t h = vr[v].dh;
+            const uint32_t h = dh[v];
             cur_var = v;
             cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-            if (!cur_is_trail) {
-                cur_wk = d.w0off[v];
-                cur_wend = d.w0off[v + 1];
-            }
             cur_counted = false;
             cur_impl_start = n_impl;
             in_scan = true;
@@ -362,16 +401,14 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         // and the depth-first walk returns to the trail)
         const bool then_trail = (depth == 0 && cur_is_trail) || (depth == 1 && !cur_is_trail && top_j >= top_e);
         if (cur_dp < 0 && cur_wk >= cur_wend) {
-            // scan finished.  One that implied nothing and is followed by trail
-            // scans leads straight to them: this round's window is those alone
-            // (as look-ahead scans, set up from the look-ahead buffer with their
-            // list heads loaded in the round's own trip), not a separate setup
             const bool next_trail_scans = then_trail && n_impl == cur_impl_start && ti < tn;
             if (!next_trail_scans) {
-                // descend into the implications it found
+                // descend into the implications the scan found
                 in_scan = false;
                 if (n_impl > cur_impl_start) {
-                    if (depth > 0 && lane == 0) stk[depth - 1] = make_int2((int)top_j, (int)top_e);
+                    // every thread records the frame (each reads back its own
+                    // write: no barrier need separate this store from the pop)
+                    if (depth > 0) stk[depth - 1] = make_int2((int)top_j, (int)top_e);
                     top_j = cur_impl_start;
                     top_e = n_impl;
                     depth++;
@@ -380,211 +417,173 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             }
         }
 
-        // ---- gather the window
+        // ---- lay out the window
+        if (tid == 0) {
+            sm.key_min = NO_CUT;
+            sm.imp_cnt = 0;
+            sm.collide = 0;
+            sm.confl_c = -1;
+        }
         int ndyn = 0;
         bool dyn_done = true;
         if (cur_dp >= 0) {
-            if (lane == 0) {
+            if (tid == 0) {
                 int32_t p = cur_dp;
-                while (p >= 0 && ndyn < 32) {
+                int k = 0;
+                while (p >= 0 && k < W) {
                     const int4 a = arena[2 * p];
-                    sm.e0[ndyn] = a;
-                    sm.e1[ndyn] = arena[2 * p + 1];
+                    sm.dyn0[k] = a;
+                    sm.dyn1[k] = arena[2 * p + 1];
                     p = a.w;
-                    sm.dp_after[ndyn] = p;
-                    ndyn++;
+                    sm.dyn_next[k] = p;
+                    k++;
                 }
-                dyn_done = p < 0;
+                sm.ndyn = k;
+                sm.dyn_done = p < 0;
             }
-            ndyn = __shfl_sync(FULL, ndyn, 0);
-            dyn_done = __shfl_sync(FULL, dyn_done, 0);
+            __syncthreads();
+            ndyn = sm.ndyn;
+            dyn_done = sm.dyn_done;
         }
-        // Window position p is evaluated by lane p.  Entries from the initial
-        // lists are loaded straight into that lane's registers (g*: the
-        // current scan, h*: the look-ahead scans), so the loads of both kinds
-        // are in flight together and nothing waits on them before the
-        // evaluation; only the added-list entries go through shared memory.
-        int nent = ndyn;
-        int take0 = 0;
-        int4 g0 = make_int4(0, 0, 0, 0), g1 = g0, h0 = g0, h1 = g0;
+        int nent = ndyn, take0 = 0;
         if (dyn_done) {
-            take0 = min(32 - nent, (int)(cur_wend - cur_wk));
-            if (lane >= nent && lane < nent + take0) {
-                const size_t w = cur_wk + (uint32_t)(lane - nent);
-                g0 = d.w0ent[2 * w];
-                g1 = d.w0ent[2 * w + 1];
-            }
+            const uint32_t left = cur_wend - cur_wk;
+            take0 = (int)((uint32_t)(W - nent) < left ? (uint32_t)(W - nent) : left);
             nent += take0;
         }
         const int nent0 = nent;
-        if (lane == 0) {
-            sm.sc_var[0] = cur_var;
-            sm.sc_begin[0] = 0;
-            sm.sc_end[0] = nent;
-        }
         int nsc = 1;
-        int my_scan = 0;
         const bool scan0_full = dyn_done && (cur_wk + (uint32_t)take0 == cur_wend);
-        if (scan0_full && then_trail && n_impl == cur_impl_start && nent < 32 && ti < tn) {
-            // following trail scans, assumed to start with an empty added list
-            // (checked in the evaluation trip)
-            const int room = 32 - nent;
-            if (ti - lb_base >= 16 && lb_base + 32 < tn) {
-                const int64_t old_base = lb_base;
-                if (ti - lb_base >= 32) {
-                    // (re)fill at ti: the buffer now, the next 16 and the
-                    // trail literals of the 16 after them in flight
-                    lb_base = ti;
-                    lb_v = 0;
-                    lb_a = lb_b = 0;
-                    if (ti + lane < tn) {
-                        const int32_t x = d.trail[tb + ti + lane];
-                        lb_v = (x > 0 ? x : -x) - 1;
-                        lb_a = d.w0off[lb_v];
-                        lb_b = d.w0off[lb_v + 1];
-                    }
-                    nx_v = 0;
-                    nx_a = nx_b = 0;
-                    if (lane < 16 && ti + 32 + lane < tn) {
-                        const int32_t x = d.trail[tb + ti + 32 + lane];
-                        nx_v = (x > 0 ? x : -x) - 1;
-                        nx_a = d.w0off[nx_v];
-                        nx_b = d.w0off[nx_v + 1];
-                    }
-                } else {
-                    // advance by 16: lanes 0-15 take lanes 16-31, lanes 16-31
-                    // the next 16 (loaded one advance ago)
-                    lb_base += 16;
-                    const int sl = (lane + 16) & 31;
-                    const int32_t hv = __shfl_sync(FULL, lb_v, sl), qv = __shfl_sync(FULL, nx_v, sl);
-                    const uint32_t ha = __shfl_sync(FULL, lb_a, sl), qa = __shfl_sync(FULL, nx_a, sl);
-                    const uint32_t hb = __shfl_sync(FULL, lb_b, sl), qb = __shfl_sync(FULL, nx_b, sl);
-                    lb_v = lane < 16 ? hv : qv;
-                    lb_a = lane < 16 ? ha : qa;
-                    lb_b = lane < 16 ? hb : qb;
-                    nx_v = 0;
-                    nx_a = nx_b = 0;
-                    if (lane < 16 && lb_base + 32 + lane < tn) {
-                        nx_v = (nnx > 0 ? nnx : -nnx) - 1;
-                        nx_a = d.w0off[nx_v];
-                        nx_b = d.w0off[nx_v + 1];
-                    }
-                }
-                nnx = 0;
-                if (lane < 16 && lb_base + 48 + lane < tn) nnx = d.trail[tb + lb_base + 48 + lane];
-                // warm L2 with the initial watch entries of the positions that
-                // entered the buffer (a line holds four): the rounds of the
-                // next trail scans gather them
-                if (lb_base + lane >= old_base + 32) {
-                    const uint32_t ne = lb_b - lb_a < 32u ? lb_b - lb_a : 32u;
-                    for (uint32_t q = 0; q < ne; q += 4)
-                        asm volatile("prefetch.global.L2 [%0];" ::"l"(d.w0ent + 2 * (size_t)(lb_a + q)));
-                }
-                // the buffer's entry stream, laid out once per refill: position
-                // j's (up to 32) entries follow position j-1's; lb_p is the
-                // inclusive prefix of the counts and q2j maps a stream offset
-                // back to its buffer position
-                const int c = (int)(lb_b - lb_a < 32u ? lb_b - lb_a : 32u);
-                int pc = c;
+        const int64_t lim = ring_hi < tn ? ring_hi : tn;
+        if (tid == 0) {
+            sm.sc_var[0] = cur_var;
+            sm.sc_b[0] = 0;
+            sm.sc_e[0] = nent0;
+        }
+        if (scan0_full && then_trail && n_impl == cur_impl_start && nent < W && ti < lim) {
+            // following trail scans from the ring: lane j of warp 0 takes
+            // position ti + j; a scan is taken if it starts inside the window
+            // (the last one may be cut short) and its variable is not already
+            // a window scan's
+            if (wid == 0) {
+                const int64_t q = ti + lane;
+                const bool in = lane < MAXSC - 1 && q < lim;
+                const int r = (int)(q & (LB - 1));
+                const int32_t v = in ? sm.lb_var[r] : -1 - lane;
+                const uint32_t a = in ? sm.lb_a[r] : 0u, b = in ? sm.lb_b[r] : 0u, h = in ? sm.lb_h[r] : 0u;
+                const bool hasA = in && (h >> 24) == e;
+                const int cnt = in ? (hasA ? 1 : 0) + (int)(b - a) : 0;
+                int incl = cnt;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(FULL, pc, o);
-                    if (lane >= o) pc += y;
+                    const int y = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += y;
                 }
-                lb_p = pc;
-                for (int q = pc - c; q < pc; q++) sm.q2j[q] = (uint8_t)lane;
-                __syncwarp();
-            }
-            const int lb_off = (int)(ti - lb_base);
-            const int64_t ahead = (32 - lb_off < tn - ti) ? (int64_t)(32 - lb_off) : tn - ti;
-            const int nlook = (int)(ahead < 31 ? ahead : 31);
-            const int src = (lb_off + lane) & 31;
-            const int32_t bv = __shfl_sync(FULL, lb_v, src);
-            const uint32_t ba = __shfl_sync(FULL, lb_a, src), bb = __shfl_sync(FULL, lb_b, src);
-            const int bp = __shfl_sync(FULL, lb_p, src);
-            // stream offset of the window's first look-ahead entry
-            const int pbase = lb_off > 0 ? __shfl_sync(FULL, lb_p, (lb_off - 1) & 31) : 0;
-            int32_t v = -1;
-            uint32_t a = 0, b = 0;
-            if (lane < nlook) {
-                v = bv;
-                a = ba;
-                b = bb;
-            }
-            const int cnt = (lane < nlook) ? (int)(b - a < 32u ? b - a : 32u) : 0;
-            const int incl = bp - pbase;  // (lanes below nlook)
-            const int excl = incl - cnt;
-            const unsigned ok = __ballot_sync(FULL, lane < nlook && excl < room);
-            const int K = (~ok) ? __ffs(~ok) - 1 : 32;
-            if (lane < K) {
-                sm.sc_var[1 + lane] = v;
-                sm.sc_begin[1 + lane] = nent + excl;
-                sm.sc_end[1 + lane] = min(nent + excl + cnt, 32);
-                sm.sc_wk[1 + lane] = a;
-                sm.sc_wend[1 + lane] = b;
-            }
-            if (K > 0) {
-                const int total = min(nent + __shfl_sync(FULL, incl, K - 1), 32);
-                // window position -> look-ahead scan, through the stream map
-                if (lane >= nent && lane < total) my_scan = 1 + (int)sm.q2j[pbase + lane - nent] - lb_off;
-                const int jj = my_scan - 1;
-                const int ej = __shfl_sync(FULL, excl, jj < 0 ? 0 : jj);
-                const uint32_t aj = __shfl_sync(FULL, a, jj < 0 ? 0 : jj);
-                if (lane >= nent && lane < total) {
-                    const size_t w = aj + (uint32_t)(lane - nent - ej);
-                    h0 = d.w0ent[2 * w];
-                    h1 = d.w0ent[2 * w + 1];
+                const int start = nent + incl - cnt;
+                const unsigned same = __match_any_sync(FULL, v);
+                const bool dup = in && ((same & lt) != 0 || v == cur_var);
+                const unsigned ok = __ballot_sync(FULL, in && start < W && !dup);
+                const int K = (~ok) ? __ffs(~ok) - 1 : 32;
+                if (lane < K) {
+                    const int s = 1 + lane;
+                    const int end = start + cnt < W ? start + cnt : W;
+                    sm.sc_var[s] = v;
+                    sm.sc_b[s] = start;
+                    sm.sc_e[s] = end;
+                    sm.sc_wk[s] = a;
+                    sm.sc_wend[s] = b;
+                    sm.sc_head[s] = hasA ? (int32_t)(h & 0xFFFFFFu) : -1;
+                    sm.sc_h[s] = h;
+                    sm.sc_next[s] = -1;
+                    for (int p = start; p < end; p++) sm.pos_scan[p] = (uint8_t)s;
                 }
-                nent = total;
-                nsc = 1 + K;
+                const int last = K > 0 ? __shfl_sync(FULL, incl, K - 1) : 0;
+                if (lane == 0) {
+                    sm.nsc = 1 + K;
+                    sm.nent = nent + last < W ? nent + last : W;
+                }
+            }
+            __syncthreads();
+            nsc = sm.nsc;
+            nent = sm.nent;
+        } else {
+            __syncthreads();
+        }
+
+        // ---- the window's entries (trip 1): thread p loads position p;
+        // thread s (1 <= s < nsc) also loads window scan s's list head again
+        const bool has = tid < nent;
+        int my_scan = 0;
+        int4 en = make_int4(0, 0, 0, 0), el = en;
+        if (has) {
+            if (tid < nent0) {
+                if (tid < ndyn) {
+                    en = sm.dyn0[tid];
+                    el = sm.dyn1[tid];
+                } else {
+                    const size_t w = cur_wk + (uint32_t)(tid - ndyn);
+                    en = d.w0ent[2 * w];
+                    el = d.w0ent[2 * w + 1];
+                }
+            } else {
+                my_scan = sm.pos_scan[tid];
+                const int q = tid - sm.sc_b[my_scan];
+                const int32_t head = sm.sc_head[my_scan];
+                if (head >= 0 && q == 0) {
+                    en = arena[2 * head];
+                    el = arena[2 * head + 1];
+                    sm.sc_next[my_scan] = en.w;
+                } else {
+                    const size_t w = sm.sc_wk[my_scan] + (uint32_t)(q - (head >= 0 ? 1 : 0));
+                    en = d.w0ent[2 * w];
+                    el = d.w0ent[2 * w + 1];
+                }
             }
         }
-        __syncwarp();
-
-        // ---- evaluate every entry of the window at once
-        const bool has = lane < nent;
-        const int4 en = lane < ndyn ? sm.e0[lane] : (lane < nent0 ? g0 : h0);
-        const int4 el = lane < ndyn ? sm.e1[lane] : (lane < nent0 ? g1 : h1);
+        uint32_t hnow = 0;
+        const bool vthr = tid >= 1 && tid < nsc;
+        if (vthr) hnow = dh[sm.sc_var[tid]];
         const int32_t sv = sm.sc_var[my_scan];
-        // lane s (1 <= s < nsc) checks whether window scan s starts with added clauses
-        const int32_t scan_v = (lane >= 1 && lane < nsc) ? sm.sc_var[lane] : -1;
-        const int32_t scan_b = (lane >= 1 && lane < nsc) ? sm.sc_begin[lane] : 0;
+
+        // ---- every entry's state (trip 2): the clause state, the assignment
+        // words of its literals and the list head of each possible move
+        // target (the literals its initial watches leave out; a clause whose
+        // watches moved that needs another head loads it at commit time)
         Eval r;
         r.act = A_NONE;
         r.acnt = 0;
         r.t1 = r.t2 = -1;
-        r.dh1 = r.dh2 = 0;
         r.unit = -1;
         r.nw1 = r.nw2 = 0;
         bool valid = false;
         int32_t ov = -1;  // a valid entry's clause: its other watched variable
         int w1 = 0, w2 = 0;
-        uint32_t scan_h = 0;
+        uint32_t dh1 = 0, dh2 = 0;
+        bool dh1_ok = false, dh2_ok = false;
         if (has) {
             const uint32_t st = cst[en.x];
             const int len = en.z;
             const int32_t Lr[KIN] = {el.x, el.y, el.z, el.w};
-            uint8_t Av[KIN];
-            uint32_t Dh[KIN];
-            // every random load of the round in one trip: clause state, the
-            // literals' assignments and list heads (unused ones are cheap misses)
+            const bool fresh = (st >> 24) != e;
+            const int iw1 = (uint32_t)en.w >> 16, iw2 = en.w & 0xFFFF;   // initial watches (static entries)
+            const bool is_added = tid < nent0 ? tid < ndyn : (sm.sc_head[my_scan] >= 0 && tid == sm.sc_b[my_scan]);
+            uint32_t Ab[KIN], Dh[KIN];
 #pragma unroll
             for (int i = 0; i < KIN; i++) {
-                // one 8-byte load per literal: list head and assignment byte
-                const uint2 rv = (i < len) ? *reinterpret_cast<const uint2 *>(&vr[Lr[i] >> 1]) : make_uint2(0, 0);
-                Av[i] = (uint8_t)(rv.y & 0xFFu);
-                Dh[i] = rv.x;
+                const int32_t v = Lr[i] >> 1;
+                Ab[i] = (i < len) ? asg_bits(asg[v >> 4], v) : 0u;
+                const bool want = i < len && len <= KIN && v != sv && (is_added || len > 3 || (i != iw1 && i != iw2));
+                Dh[i] = want ? dh[v] : 0u;
             }
-            if (scan_v >= 0) scan_h = vr[scan_v].dh;
             bool blk;
-            if ((st >> 24) == e) {
+            if (!fresh) {
                 blk = (st >> 22) & 1u;
                 w1 = (st >> 11) & 0x7FFu;
                 w2 = st & 0x7FFu;
             } else {
                 blk = false;
-                w1 = (uint32_t)en.w >> 16;
-                w2 = en.w & 0xFFFF;
+                w1 = iw1;
+                w2 = iw2;
             }
             if (len <= KIN) {
                 int32_t l1 = 0, l2 = 0;
@@ -593,11 +592,11 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 for (int i = 0; i < KIN; i++) {
                     if (i == w1) {
                         l1 = Lr[i];
-                        c1 = cons_of(Av[i], Lr[i], e);
+                        c1 = cons_of(Ab[i], Lr[i]);
                     }
                     if (i == w2) {
                         l2 = Lr[i];
-                        c2 = cons_of(Av[i], Lr[i], e);
+                        c2 = cons_of(Ab[i], Lr[i]);
                     }
                 }
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
@@ -607,41 +606,46 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                     if (!(c1 && c2)) {
                         int pend = (!c1 && !c2) ? 2 : 1, f1 = -1, f2 = -1;
                         int32_t lf1 = 0, lf2 = 0;
-                        uint32_t df1 = 0, df2 = 0;
-                        uint8_t af1 = 0;
+                        uint32_t af1 = 0, df1 = 0, df2 = 0;
+                        bool ok1 = false, ok2 = false;
 #pragma unroll
                         for (int i = 0; i < KIN; i++) {
                             if (i < len && pend > 0 && i != w1 && i != w2) {
                                 r.acnt++;
-                                if (cons_of(Av[i], Lr[i], e)) {
+                                if (cons_of(Ab[i], Lr[i])) {
+                                    const bool loaded =
+                                        (Lr[i] >> 1) != sv && (is_added || len > 3 || (i != iw1 && i != iw2));
                                     if (f1 < 0) {
                                         f1 = i;
                                         lf1 = Lr[i];
+                                        af1 = Ab[i];
                                         df1 = Dh[i];
-                                        af1 = Av[i];
+                                        ok1 = loaded;
                                     } else {
                                         f2 = i;
                                         lf2 = Lr[i];
                                         df2 = Dh[i];
+                                        ok2 = loaded;
                                     }
                                     pend--;
                                 }
                             }
                         }
                         int32_t unit = -1;
-                        uint8_t au = 0;
+                        uint32_t au = 0;
                         if (c1 || c2) {
                             if (f1 < 0) {
                                 unit = c1 ? l1 : l2;
 #pragma unroll
                                 for (int i = 0; i < KIN; i++)
-                                    if (i == (c1 ? w1 : w2)) au = Av[i];
+                                    if (i == (c1 ? w1 : w2)) au = Ab[i];
                             } else {
                                 r.act = A_SW1;
                                 r.nw1 = c1 ? w1 : f1;
                                 r.nw2 = c1 ? f1 : w2;
                                 r.t1 = lf1 >> 1;
-                                r.dh1 = df1;
+                                dh1 = df1;
+                                dh1_ok = ok1;
                             }
                         } else if (f1 >= 0 && f2 >= 0) {
                             r.act = A_SW2;
@@ -649,8 +653,10 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                             r.nw2 = f2;
                             r.t1 = lf1 >> 1;
                             r.t2 = lf2 >> 1;
-                            r.dh1 = df1;
-                            r.dh2 = df2;
+                            dh1 = df1;
+                            dh2 = df2;
+                            dh1_ok = ok1;
+                            dh2_ok = ok2;
                         } else if (f1 >= 0) {
                             unit = lf1;
                             au = af1;
@@ -659,7 +665,7 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                         }
                         if (unit >= 0) {
                             r.unit = unit;
-                            r.act = ((uint32_t)(au >> 1) != e) ? A_IMPLY : A_BLOCK;
+                            r.act = (au & 1u) ? A_BLOCK : A_IMPLY;
                         }
                     }
                 }
@@ -667,154 +673,206 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
                 const int32_t l1 = d.lits[en.y + w1], l2 = d.lits[en.y + w2];
                 valid = !blk && ((l1 >> 1) == sv || (l2 >> 1) == sv);
                 if (valid) ov = ((l1 >> 1) == sv) ? (l2 >> 1) : (l1 >> 1);
-                if (valid) eval_long(d, vr, en.y, len, w1, w2, e, r);
+                if (valid) eval_long(d, asg, en.y, len, w1, w2, r);
             }
-        } else if (scan_v >= 0) {
-            scan_h = vr[scan_v].dh;
         }
 
         // ---- where the commit stops: the smallest event key of the round
         int key = NO_CUT;
-        {
-            // an entry whose clause an earlier entry of the round also holds
-            // (and may change).  A clause is listed once per variable and only
-            // a valid entry acts, so that is a valid entry whose clause's other
-            // watched variable is an earlier window scan's (scan 0: checked
-            // here; later scans: in the loop below).  Scan 0 may have entries
-            // from earlier rounds, so this can cut where nothing repeats: a
-            // cut only ends the round early.
-            if (valid && my_scan > 0 && ov == cur_var) key = key_before(lane, my_scan);
-            if (valid && r.act == A_CONFLICT) key = min(key, key_after(lane, my_scan));
-            // an implication ends its scan's part of the window (its depth-first
-            // descent comes before any later scan) ...
-            const bool imp = valid && r.act == A_IMPLY;
-            if (imp) key = min(key, key_after(sm.sc_end[my_scan] - 1, my_scan));
-            // ... and a later entry of the same scan is evaluated again if its
-            // clause has the implied variable (a long clause: always); the
-            // other entries read nothing the implication changed
-            unsigned im = __ballot_sync(FULL, imp);
-            while (im) {
-                const int k = __ffs(im) - 1;
-                im &= im - 1;
-                const int32_t uv = __shfl_sync(FULL, r.unit >> 1, k);
-                const int ks = __shfl_sync(FULL, my_scan, k);
-                if (valid && lane > k && my_scan == ks) {
-                    const bool dep = en.z > KIN || (el.x >> 1) == uv || (en.z > 1 && (el.y >> 1) == uv) ||
-                                     (en.z > 2 && (el.z >> 1) == uv) || (en.z > 3 && (el.w >> 1) == uv);
-                    if (dep) key = min(key, key_before(lane, my_scan));
-                }
+        // a following scan whose list is not what the layout assumed
+        if (vthr) {
+            const uint32_t ha = sm.sc_h[tid];
+            const bool va = (ha >> 24) == e, vn = (hnow >> 24) == e;
+            if (va != vn || (vn && hnow != ha)) key = key_before(sm.sc_b[tid], tid);
+        }
+        // a following scan's added head with more added entries behind it:
+        // only the head is in the window
+        if (has && my_scan > 0 && tid == sm.sc_b[my_scan] && sm.sc_head[my_scan] >= 0 && en.w >= 0)
+            key = min(key, key_before(tid + 1, my_scan));
+        const bool mv = valid && (r.act == A_SW1 || r.act == A_SW2);
+        if (valid) {
+            // an entry whose clause an earlier window scan also holds (and may
+            // change): a clause is listed under the two variables it watches,
+            // so that is one whose other watched variable is an earlier window
+            // scan's (for scan 0, whose entries may come from earlier rounds,
+            // this can cut where nothing repeats: a cut only ends the round early)
+            if (my_scan > 0 && ov == cur_var) key = min(key, key_before(tid, my_scan));
+            if (r.act == A_CONFLICT) key = min(key, key_after(tid, my_scan));
+            if (r.act == A_IMPLY) {
+                // an implication ends its scan's part of the window
+                key = min(key, key_after(sm.sc_e[my_scan] - 1, my_scan));
+                const int k = atomicAdd(&sm.imp_cnt, 1);
+                sm.imp_pos[k] = (int16_t)tid;
+                sm.imp_scan[k] = (int8_t)my_scan;
+                sm.imp_var[k] = r.unit >> 1;
             }
-            // a later window scan whose list starts with added clauses
-            if (scan_v >= 0 && (scan_h >> 24) == e) key = min(key, key_before(scan_b, lane));
-            // a move of this lane that lands in a later window scan's list, and
-            // the repeated clauses of scans 1.. (lane s holds window scan s's
-            // variable and start; the loop is uniform, so its shuffles are
-            // independent and overlap, and the smallest key is the first scan)
-            const bool mv = valid && (r.act == A_SW1 || r.act == A_SW2);
-            if (nsc > 1) {
-                for (int s = 1; s < nsc; s++) {
-                    const int32_t vs = __shfl_sync(FULL, scan_v, s);
-                    const int bs = __shfl_sync(FULL, scan_b, s);
-                    if (mv && s > my_scan && (vs == r.t1 || vs == r.t2)) key = min(key, key_before(bs, s));
-                    if (valid && s < my_scan && vs == ov) key = min(key, key_before(lane, my_scan));
-                }
+            for (int s = 1; s < nsc; s++) {
+                const int32_t vs = sm.sc_var[s];
+                if (s < my_scan && vs == ov) key = min(key, key_before(tid, my_scan));
+                // a move into a later window scan's list
+                if (mv && s > my_scan && (vs == r.t1 || vs == r.t2)) key = min(key, key_before(sm.sc_b[s], s));
             }
         }
-        const int cut = __reduce_min_sync(FULL, key);
+        __syncthreads();
+        // a later entry of an implying scan whose clause has the implied variable
+        // (a long clause: always); the other entries read nothing the
+        // implication changed, so several implications commit in one round
+        const int nimp = sm.imp_cnt;
+        if (valid && nimp > 0) {
+            for (int j = 0; j < nimp; j++) {
+                if (sm.imp_scan[j] != my_scan || sm.imp_pos[j] >= tid) continue;
+                const int32_t uv = sm.imp_var[j];
+                const bool dep = en.z > KIN || (el.x >> 1) == uv || (en.z > 1 && (el.y >> 1) == uv) ||
+                                 (en.z > 2 && (el.z >> 1) == uv) || (en.z > 3 && (el.w >> 1) == uv);
+                if (dep) key = min(key, key_before(tid, my_scan));
+            }
+        }
+        const int cut = block_min(sm, key);
         int k_end, new_cur;
         bool new_started;
         if (cut == NO_CUT) {
             k_end = nent;
             new_cur = nsc - 1;
-            new_started = (new_cur == 0) || (sm.sc_end[new_cur] > sm.sc_begin[new_cur]);
+            new_started = (new_cur == 0) || (sm.sc_e[new_cur] > sm.sc_b[new_cur]);
         } else {
             k_end = cut >> 7;
             new_cur = (cut >> 1) & 63;
-            new_started = (cut & 1) || new_cur == 0 || k_end > sm.sc_begin[new_cur];
+            new_started = (cut & 1) || new_cur == 0 || k_end > sm.sc_b[new_cur];
+        }
+        // a round that would commit nothing and start no scan could never end
+        // the trail: report it (it cannot happen; the guard keeps a fault in
+        // this logic from spinning until the iteration budget runs out)
+        if (k_end == 0 && new_cur == 0) {
+            status = GPSAT_BCP_BUDGET;
+            stopi = (int32_t)cur_trail;
+            break;
         }
 
+        // ---- ranks of the committed implications and moves (window order)
+        bool com = valid && tid < k_end;
+        int tot_im = 0, tot_mv = 0, my_im = 0, my_mv = 0;
+        auto rank = [&]() {
+            const bool imp = com && r.act == A_IMPLY;
+            const unsigned bi = __ballot_sync(FULL, imp);
+            const unsigned b1 = __ballot_sync(FULL, com && (r.act == A_SW1 || r.act == A_SW2));
+            const unsigned b2 = __ballot_sync(FULL, com && r.act == A_SW2);
+            if (lane == 0) {
+                sm.wcnt_im[wid] = __popc(bi);
+                sm.wcnt_mv[wid] = __popc(b1) + __popc(b2);
+            }
+            __syncthreads();
+            int bim = 0, bmv = 0;
+            tot_im = tot_mv = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                const int ci = sm.wcnt_im[w], cm = sm.wcnt_mv[w];
+                if (w < wid) {
+                    bim += ci;
+                    bmv += cm;
+                }
+                tot_im += ci;
+                tot_mv += cm;
+            }
+            my_im = bim + __popc(bi & lt);
+            my_mv = bmv + __popc(b1 & lt) + __popc(b2 & lt);
+            __syncthreads();   // the counts are read before anyone writes them again
+        };
+        rank();
         // more implications than impl_cap leaves room for: commit up to the
         // first one that does not fit; the next round reports the overflow there
         {
-            const unsigned im0 = __ballot_sync(FULL, valid && lane < k_end && r.act == A_IMPLY);
             const int64_t room = d.impl_cap - n_impl;
-            if (room > 0 && __popc(im0) > room) {
-                const int kk = nth_set_bit(im0, (int)room + 1);
-                const int ks = __shfl_sync(FULL, my_scan, kk);
-                k_end = kk;
-                new_cur = ks;
-                new_started = ks == 0 || kk > sm.sc_begin[ks];
-            }
-        }
-        const bool com = valid && lane < k_end;
-        // watch moves: add_first into the target var's list, in commit order
-        const bool ins1 = com && (r.act == A_SW1 || r.act == A_SW2);
-        const bool ins2 = com && r.act == A_SW2;
-        const unsigned m1 = __ballot_sync(FULL, ins1), m2 = __ballot_sync(FULL, ins2);
-        const int total_ins = __popc(m1) + __popc(m2);
-        if (arena_used + total_ins > d.arena_cap) {
-            const int ks = __shfl_sync(FULL, my_scan, __ffs(m1) - 1);
-            status = GPSAT_BCP_OVERFLOW;
-            stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
-            break;
-        }
-        const unsigned imask = __ballot_sync(FULL, com && r.act == A_IMPLY);
-        if (imask && n_impl >= d.impl_cap) {
-            // stop index: the trail literal whose propagation overflowed
-            const int ks = __shfl_sync(FULL, my_scan, __ffs(imask) - 1);
-            status = GPSAT_BCP_OVERFLOW;
-            stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
-            break;
-        }
-        if (m2 == 0) {
-            const int myidx = (int)arena_used + __popc(m1 & lt);
-            const unsigned g = __match_any_sync(FULL, ins1 ? r.t1 : -1 - lane);
-            if (ins1) {
-                const unsigned before = g & lt;
-                int32_t next;
-                if (before) {
-                    const int pl = 31 - __clz(before);
-                    next = (int)arena_used + __popc(m1 & ((1u << pl) - 1u));
-                } else {
-                    next = ((r.dh1 >> 24) == e) ? (int32_t)(r.dh1 & 0xFFFFFFu) : -1;
+            if (room > 0 && tot_im > room) {
+                if (com && r.act == A_IMPLY && my_im == room) {
+                    sm.nent = tid;
+                    sm.nsc = my_scan;
                 }
-                arena[2 * myidx] = make_int4(en.x, en.y, en.z, next);
-                arena[2 * myidx + 1] = el;
-                if ((g & lanemask_gt()) == 0) vr[r.t1].dh = (e << 24) | (uint32_t)myidx;
+                __syncthreads();
+                k_end = sm.nent;
+                new_cur = sm.nsc;
+                new_started = new_cur == 0 || k_end > sm.sc_b[new_cur];
+                com = valid && tid < k_end;
+                rank();
             }
-        } else {
-            // rare (a clause moving both watches needs 4+ literals): lane 0
-            // inserts every move serially, in commit order
-            int idx = (int)arena_used;
-            unsigned rem = m1;
-            while (rem) {
-                const int k = __ffs(rem) - 1;
-                rem &= rem - 1;
-                const int32_t c = __shfl_sync(FULL, en.x, k), off = __shfl_sync(FULL, en.y, k),
-                              len = __shfl_sync(FULL, en.z, k);
-                const int4 lk = make_int4(__shfl_sync(FULL, el.x, k), __shfl_sync(FULL, el.y, k),
-                                          __shfl_sync(FULL, el.z, k), __shfl_sync(FULL, el.w, k));
-                const int32_t tt1 = __shfl_sync(FULL, r.t1, k), tt2 = __shfl_sync(FULL, r.t2, k);
-                const bool two = (m2 >> k) & 1u;
-                if (lane == 0) {
-                    uint32_t h = vr[tt1].dh;
-                    int32_t next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-                    arena[2 * idx] = make_int4(c, off, len, next);
-                    arena[2 * idx + 1] = lk;
-                    vr[tt1].dh = (e << 24) | (uint32_t)idx;
-                    if (two) {
-                        h = vr[tt2].dh;
-                        next = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
-                        arena[2 * (idx + 1)] = make_int4(c, off, len, next);
-                        arena[2 * (idx + 1) + 1] = lk;
-                        vr[tt2].dh = (e << 24) | (uint32_t)(idx + 1);
+        }
+        const int64_t ti_round = ti;
+        const bool aover = arena_used + tot_mv > d.arena_cap, iover = tot_im > 0 && n_impl >= d.impl_cap;
+        if (aover || iover) {
+            // the scan of the first move (arena) or implication (list) that
+            // does not fit; its trail position is the stop index
+            const bool first = aover ? (com && (r.act == A_SW1 || r.act == A_SW2) && my_mv == 0)
+                                     : (com && r.act == A_IMPLY && my_im == 0);
+            if (first) sm.nsc = my_scan;
+            __syncthreads();
+            const int ks = sm.nsc;
+            status = GPSAT_BCP_OVERFLOW;
+            stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
+            break;
+        }
+
+        // ---- commit
+        // moves into the same variable within the round (rare) are linked by
+        // thread 0 in window order; otherwise every mover links its own entry
+        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
+            const int32_t tg[2] = {r.t1, r.t2};
+            for (int k = 0; k < (r.act == A_SW2 ? 2 : 1); k++) {
+                const uint32_t hsh = ((uint32_t)tg[k] * 2654435761u) >> 24;
+                for (int probe = 0; probe < 2 * W; probe++) {
+                    const int slotp = (int)((hsh + (uint32_t)probe) & (2 * W - 1));
+                    const int32_t old = atomicCAS(&sm.mh[slotp], -1, tg[k]);
+                    if (old == -1) break;
+                    if (old == tg[k]) {
+                        sm.collide = 1;
+                        break;
                     }
                 }
-                idx += two ? 2 : 1;
             }
         }
-        arena_used += total_ins;
-
+        sm.mv_t1[tid] = (com && (r.act == A_SW1 || r.act == A_SW2)) ? r.t1 : -1;
+        sm.mv_t2[tid] = (com && r.act == A_SW2) ? r.t2 : -1;
+        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
+            sm.dyn0[tid] = make_int4(en.x, en.y, en.z, 0);
+            sm.dyn1[tid] = el;
+        }
+        __syncthreads();
+        const bool collide = sm.collide != 0;
+        if (!collide) {
+            if (com && (r.act == A_SW1 || r.act == A_SW2)) {
+                const int idx = (int)arena_used + my_mv;
+                if (!dh1_ok) dh1 = dh[r.t1];
+                const int32_t nx1 = ((dh1 >> 24) == e) ? (int32_t)(dh1 & 0xFFFFFFu) : -1;
+                arena[2 * idx] = make_int4(en.x, en.y, en.z, nx1);
+                arena[2 * idx + 1] = el;
+                dh[r.t1] = (e << 24) | (uint32_t)idx;
+                if (r.act == A_SW2) {
+                    if (!dh2_ok) dh2 = dh[r.t2];
+                    const int32_t nx2 = ((dh2 >> 24) == e) ? (int32_t)(dh2 & 0xFFFFFFu) : -1;
+                    arena[2 * (idx + 1)] = make_int4(en.x, en.y, en.z, nx2);
+                    arena[2 * (idx + 1) + 1] = el;
+                    dh[r.t2] = (e << 24) | (uint32_t)(idx + 1);
+                }
+            }
+        } else if (tid == 0) {
+            int idx = (int)arena_used;
+            for (int p = 0; p < k_end; p++) {
+                const int32_t tg1 = sm.mv_t1[p];
+                if (tg1 < 0) continue;
+                const int4 a = sm.dyn0[p], b = sm.dyn1[p];
+                const int32_t tg2 = sm.mv_t2[p];
+                uint32_t h = dh[tg1];
+                arena[2 * idx] = make_int4(a.x, a.y, a.z, ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1);
+                arena[2 * idx + 1] = b;
+                dh[tg1] = (e << 24) | (uint32_t)idx;
+                idx++;
+                if (tg2 >= 0) {
+                    h = dh[tg2];
+                    arena[2 * idx] = make_int4(a.x, a.y, a.z, ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1);
+                    arena[2 * idx + 1] = b;
+                    dh[tg2] = (e << 24) | (uint32_t)idx;
+                    idx++;
+                }
+            }
+        }
         // clause states
         if (com && r.act != A_NONE) {
             uint32_t ns;
@@ -822,31 +880,71 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             else ns = (e << 24) | (1u << 22) | ((uint32_t)w1 << 11) | (uint32_t)w2;
             cst[en.x] = ns;
         }
-        // implications, in commit order (all of one scan, on distinct variables)
-        if (imask) {
-            if ((imask >> lane) & 1u) {
-                const int64_t at = n_impl + __popc(imask & lt);
-                ilit[at] = dimacs_of(r.unit);
-                ireason[at] = en.x;
-                vr[r.unit >> 1].asg = (uint8_t)((e << 1) | (uint32_t)(r.unit & 1));
-            }
-            n_impl += __popc(imask);
-            cI += __popc(imask);
+        // implications, in window order (all of one scan, on distinct variables)
+        if (com && r.act == A_IMPLY) {
+            const int64_t at = n_impl + my_im;
+            ilit[at] = dimacs_of(r.unit);
+            ireason[at] = en.x;
+            impl[at] = r.unit;
+            const int32_t u = r.unit >> 1;
+            atomicOr(&asg[u >> 4], ((r.unit & 1) ? 3u : 1u) << ((u & 15) << 1));
         }
-        const unsigned cmask = __ballot_sync(FULL, com && r.act == A_CONFLICT);
+        if (com && r.act == A_CONFLICT) {
+            sm.confl_c = en.x;
+            sm.confl_scan = my_scan;
+        }
         if (com) {
             myW++;
             myL += en.z;
             myA += r.acnt;
         }
-        const int64_t ti_round = ti;
-        __syncwarp();
+        // the look-ahead ring: warp 1 publishes the chunk it loaded a refill
+        // ago and starts the next two (the decision is the same in every thread)
+        const bool refill = ring_hi < tn && ring_hi - ti < LEAD;
+        if (refill && wid == 1) {
+            // stage 2 -> ring
+            const int64_t q = ring_hi + lane;
+            if (q < tn) {
+                const int rr = (int)(q & (LB - 1));
+                sm.lb_var[rr] = pipe.var;
+                sm.lb_a[rr] = pipe.a;
+                sm.lb_b[rr] = pipe.b;
+                sm.lb_h[rr] = pipe.h;
+                // warm L2 with the position's initial watch entries (two per line)
+                const uint32_t ne = pipe.b - pipe.a < 32u ? pipe.b - pipe.a : 32u;
+                for (uint32_t k = 0; k < ne; k += 2)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.w0ent + 2 * (size_t)(pipe.a + k)));
+            }
+            // stage 1 -> stage 2, and a new stage 1
+            const int64_t nb = ring_hi + CHUNK;
+            if (nb < tn) {
+                const int64_t q2 = nb + lane;
+                if (q2 < tn) {
+                    int32_t v = (pipe.lit > 0 ? pipe.lit : -pipe.lit) - 1;
+                    if (v < 0 || v >= n) v = 0;
+                    pipe.var = v;
+                    pipe.a = d.w0off[v];
+                    pipe.b = d.w0off[v + 1];
+                    pipe.h = dh[v];
+                }
+                const int64_t q3 = nb + CHUNK + lane;
+                if (q3 < tn) pipe.lit = d.trail[tb + q3];
+            }
+        }
+        if (refill) ring_hi = ring_hi + CHUNK < tn ? ring_hi + CHUNK : tn;
+        __syncthreads();
+        // empty the move-target table for the next round (the end-of-round
+        // barrier separates this from the next round's inserts)
+        for (int i = tid; i < 2 * W; i += NT) sm.mh[i] = -1;
+        arena_used += tot_mv;
+        n_impl += tot_im;
+        cI += tot_im;
 
         // ---- advance the scan cursors
         if (new_cur == 0) {
             if (k_end > 0) {
                 if (k_end <= ndyn) {
-                    cur_dp = sm.dp_after[k_end - 1];
+                    cur_dp = sm.dyn_next[k_end - 1];
                 } else {
                     cur_dp = -1;
                     cur_wk += (uint32_t)(k_end - ndyn);
@@ -855,15 +953,24 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         } else {
             props += new_cur - 1;
             cur_var = sm.sc_var[new_cur];
+            cur_wk = sm.sc_wk[new_cur];
+            cur_wend = sm.sc_wend[new_cur];
             cur_dp = -1;
             if (!new_started) {
-                // cut before this scan because its list starts with added
-                // clauses (possibly added by this round): those come first
-                const uint32_t h = vr[cur_var].dh;
+                // cut before this scan because its list is not what the window
+                // assumed (possibly changed by this round): read it again
+                const uint32_t h = dh[cur_var];
                 cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+            } else {
+                const int k = k_end - sm.sc_b[new_cur];
+                if (sm.sc_head[new_cur] >= 0) {
+                    const int32_t nx = sm.sc_next[new_cur];
+                    if (nx >= 0) cur_dp = nx;   // cut right after the head
+                    else cur_wk += (uint32_t)(k - 1);
+                } else {
+                    cur_wk += (uint32_t)k;
+                }
             }
-            cur_wk = sm.sc_wk[new_cur] + (uint32_t)(k_end - sm.sc_begin[new_cur]);
-            cur_wend = sm.sc_wend[new_cur];
             cur_counted = new_started;
             if (new_started) props++;
             cur_trail = ti + new_cur - 1;
@@ -871,22 +978,42 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
             ti += new_cur;
             cur_is_trail = true;
             depth = 0;  // a descent whose scan led into trail scans has ended
-            cur_impl_start = n_impl - __popc(imask);
+            cur_impl_start = n_impl - tot_im;
         }
-        if (cmask) {
-            const int k = __ffs(cmask) - 1;
-            confl = __shfl_sync(FULL, en.x, k);
-            const int ks = __shfl_sync(FULL, my_scan, k);
+        const int32_t cc = sm.confl_c;
+        if (cc >= 0) {
+            const int ks = sm.confl_scan;
+            confl = cc;
             stopi = (int32_t)(ks == 0 ? (new_cur == 0 ? cur_trail : dfs_trail) : ti_round + ks - 1);
             status = GPSAT_BCP_CONFLICT;
         }
-        __syncwarp();
+        __syncthreads();   // the window's shared state is read before the next round rewrites it
     }
 
+    // ---- clear the assignment words this trail set (trail and implications)
+    for (int64_t i = tid; i < tn; i += NT) {
+        const int32_t x = d.trail[tb + i];
+        if (x != 0 && x <= n && x >= -n) asg[((x > 0 ? x : -x) - 1) >> 4] = 0u;
+    }
+    for (int64_t i = tid; i < n_impl; i += NT) asg[(impl[i] >> 1) >> 4] = 0u;
+
+    // ---- outputs
     myW = warp_sum(myW);
     myL = warp_sum(myL);
     myA = warp_sum(myA);
     if (lane == 0) {
+        sm.red[wid][0] = (unsigned long long)myW;
+        sm.red[wid][1] = (unsigned long long)myL;
+        sm.red[wid][2] = (unsigned long long)myA;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int64_t W_ = 0, L_ = 0, A_ = 0;
+        for (int w = 0; w < NW; w++) {
+            W_ += (int64_t)sm.red[w][0];
+            L_ += (int64_t)sm.red[w][1];
+            A_ += (int64_t)sm.red[w][2];
+        }
         d.status[t] = status;
         d.conflict[t] = confl;
         d.stop[t] = stopi;
@@ -894,13 +1021,14 @@ __device__ void process_trail(const Dev &d, WarpSmem &sm, int t, int slot, int l
         if (d.counters) {
             int64_t *cn = d.counters + (size_t)t * GPSAT_BCP_NCOUNTERS;
             cn[0] = props;
-            cn[1] = myW;
-            cn[2] = myL;
-            cn[3] = myA;
+            cn[1] = W_;
+            cn[2] = L_;
+            cn[3] = A_;
             cn[4] = cI;
             cn[5] = bad ? 0 : tn;
         }
     }
+    __syncthreads();   // the bitmap is clean and the shared state free before the next trail
 }
 
 // ---------------------------------------------------------------------------
@@ -959,24 +1087,23 @@ __global__ void order_scatter(const int64_t *toff, int T, unsigned *hist, int32_
         order[atomicAdd(&hist[order_bucket(toff, t)], 1u)] = t;
 }
 
-// blocks per SM the register allocation targets: 4 (16 resident warps per SM)
-// leaves the kernel its ~100 registers without spills, which measured faster
-// than 32 resident warps with spills at 64 registers
+// blocks per SM the register allocation targets
 #ifndef GPSAT_BCP_MIN_BLOCKS
 #define GPSAT_BCP_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(WARPS * 32, GPSAT_BCP_MIN_BLOCKS) bcp_kernel(Dev d)
+__global__ void __launch_bounds__(NT, GPSAT_BCP_MIN_BLOCKS) bcp_kernel(Dev d)
 {
-    __shared__ WarpSmem smem[WARPS];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int slot = blockIdx.x * WARPS + wib;
+    __shared__ Smem sm;
+    for (int i = threadIdx.x; i < 2 * W; i += NT) sm.mh[i] = -1;
+    const int slot = blockIdx.x;
     if (slot >= d.n_slots) return;
+    __syncthreads();
     while (true) {
-        int t = 0;
-        if (lane == 0) t = (int)atomicAdd(d.next_trail, 1u);
-        t = __shfl_sync(FULL, t, 0);
+        if (threadIdx.x == 0) sm.t = (int)atomicAdd(d.next_trail, 1u);
+        __syncthreads();
+        const int t = sm.t;
         if (t >= d.n_trails) break;
-        process_trail(d, smem[wib], d.order ? d.order[t] : t, slot, lane);
+        process_trail(d, sm, d.order ? d.order[t] : t, slot);
     }
 }
 
@@ -993,11 +1120,11 @@ struct gpsat_bcp {
     int device = 0;
     int32_t slots = 0;
     int32_t active = 0;                // slots the launches use (0: all)
-    int64_t n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
-    bcp::VarRec *vr = nullptr;
-    uint32_t *cst = nullptr, *epoch = nullptr;
+    int64_t n_words = 0, n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
+    uint32_t *asg = nullptr, *dh = nullptr, *cst = nullptr, *epoch = nullptr;
     int4 *arena = nullptr;
     int2 *stack = nullptr;
+    int32_t *impl = nullptr;
     unsigned int *counter = nullptr;
     unsigned *hist = nullptr;          // ORDER_BUCKETS counters
     int32_t *order = nullptr;          // processing order of the last launch
@@ -1015,8 +1142,10 @@ namespace {
 
 void bcp_free(gpsat_bcp *b)
 {
-    cudaFree(b->vr);
+    cudaFree(b->asg);
+    cudaFree(b->dh);
     cudaFree(b->cst);
+    cudaFree(b->impl);
     cudaFree(b->epoch);
     cudaFree(b->arena);
     cudaFree(b->stack);
@@ -1039,12 +1168,15 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
     d.lits = f->d_lits;
     d.w0off = f->d_w0off;
     d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
-    d.vr = b->vr;
+    d.asg = b->asg;
+    d.dh = b->dh;
     d.cst = b->cst;
     d.arena = b->arena;
     d.stack = b->stack;
+    d.impl = b->impl;
     d.epoch = b->epoch;
     d.next_trail = b->counter;
+    d.n_words = b->n_words;
     d.n_pad = b->n_pad;
     d.m_pad = b->m_pad;
     d.arena_cap = b->arena_cap;
@@ -1084,8 +1216,7 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
         bcp::order_scatter<<<g, 256, 0, st>>>(toff, n_trails, b->hist, b->order);
         d.order = b->order;
     }
-    const int blocks = (d.n_slots + bcp::WARPS - 1) / bcp::WARPS;
-    bcp::bcp_kernel<<<blocks, bcp::WARPS * 32, 0, st>>>(d);
+    bcp::bcp_kernel<<<d.n_slots, bcp::NT, 0, st>>>(d);
     err = cudaGetLastError();
     if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch");
     return GPSAT_OK;
@@ -1108,16 +1239,17 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
     if (urc != GPSAT_OK) return urc;
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::WARPS * 32, 0);
-    int32_t resident = std::max(1, sms * std::max(per_sm, 1) * bcp::WARPS);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::NT, 0);
+    int32_t resident = std::max(1, sms * std::max(per_sm, 1));
     gpsat_bcp *b = new gpsat_bcp();
     b->f = f;
     b->device = f->device;
     b->n_pad = ((int64_t)f->h.n_vars + 15) / 16 * 16;
+    b->n_words = b->n_pad / 16;
     b->m_pad = (f->h.n_clauses() + 3) / 4 * 4;
     b->impl_cap = impl_cap;
     b->arena_cap = arena_cap ? arena_cap : (1 << 17);
-    const int64_t per_slot = b->n_pad * 8 + b->m_pad * 4 + b->arena_cap * 32 + b->impl_cap * 8;
+    const int64_t per_slot = b->n_words * 4 + b->n_pad * 4 + b->m_pad * 4 + b->arena_cap * 32 + b->impl_cap * 12;
     int32_t slots = max_slots ? max_slots : resident;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -1125,14 +1257,17 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
     if ((int64_t)slots * per_slot > budget) slots = (int32_t)std::max<int64_t>(1, budget / per_slot);
     b->slots = slots;
     const size_t S = (size_t)slots;
-    bool ok = cudaMalloc(&b->vr, S * b->n_pad * 8) == cudaSuccess &&
+    bool ok = cudaMalloc(&b->asg, S * b->n_words * 4) == cudaSuccess &&
+              cudaMalloc(&b->dh, S * b->n_pad * 4) == cudaSuccess &&
               cudaMalloc(&b->cst, S * b->m_pad * 4) == cudaSuccess &&
               cudaMalloc(&b->epoch, S * 4) == cudaSuccess &&
               cudaMalloc(&b->arena, S * b->arena_cap * 32) == cudaSuccess &&
               cudaMalloc(&b->stack, S * b->impl_cap * 8) == cudaSuccess &&
+              cudaMalloc(&b->impl, S * b->impl_cap * 4) == cudaSuccess &&
               cudaMalloc(&b->counter, 16) == cudaSuccess;
     if (ok)
-        ok = cudaMemset(b->vr, 0, S * b->n_pad * 8) == cudaSuccess &&
+        ok = cudaMemset(b->asg, 0, S * b->n_words * 4) == cudaSuccess &&
+             cudaMemset(b->dh, 0, S * b->n_pad * 4) == cudaSuccess &&
              cudaMemset(b->cst, 0, S * b->m_pad * 4) == cudaSuccess && cudaMemset(b->epoch, 0, S * 4) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -1310,10 +1445,15 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
 // and hosts whose device memory is reserved up front by their own pool.  The
 // call below makes no allocating CUDA call and no library allocation; the
 // slots' state lives in bcp_static_scratch, laid out afresh by every call:
-//   [launch counter | epoch per slot | variable records | cst | move arena | stack]
-// each part 256-byte aligned.  Everything but the arena and the stack (which
-// the kernel writes before it reads) is cleared on the stream per call.  One
-// array per device, so calls whose GPU work overlaps race on it.
+//   [launch counter | epoch per slot | assignment words | list heads | clause
+//    states | move arena | stack | implied literals]
+// each part 256-byte aligned.  Everything but the arena, the stack and the
+// implied literals (which the kernel writes before it reads) is cleared on the
+// stream per call.  One array per device, so calls whose GPU work overlaps
+// race on it.  The array's device address is looked up once per device and
+// kept for the life of the process; after a cudaDeviceReset the module may be
+// loaded again at another address, so this entry is not for use across a
+// device reset.
 namespace gpsat {
 namespace bcp {
 
@@ -1358,10 +1498,10 @@ int static_setup(int device, unsigned char **base, int32_t *resident)
         int sms = 0, per_sm = 0;
         err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         if (err != cudaSuccess) return cuda_error(err, "cudaDeviceGetAttribute");
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::WARPS * 32, 0);
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::bcp_kernel, bcp::NT, 0);
         if (err != cudaSuccess) return cuda_error(err, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
         s.base[device] = static_cast<unsigned char *>(ptr);
-        s.resident[device] = std::max(1, sms * std::max(per_sm, 1) * bcp::WARPS);
+        s.resident[device] = std::max(1, sms * std::max(per_sm, 1));
         s.ready[device] = true;
     }
     *base = s.base[device];
@@ -1369,11 +1509,14 @@ int static_setup(int device, unsigned char **base, int32_t *resident)
     return GPSAT_OK;
 }
 
-// Bytes of the scratch layout for S slots (each part rounded up to 256).
+// Bytes of the scratch layout for S slots (each part rounded up to 256):
+// counter, epochs, assignment words, list heads, clause states, move arena,
+// depth-first stack, implied literals.
 int64_t static_layout_bytes(int64_t S, int64_t n_pad, int64_t m_pad, int64_t arena_cap, int64_t impl_cap)
 {
-    return STATIC_ALIGN + align_up(S * 4) + align_up(S * n_pad * 8) + align_up(S * m_pad * 4) +
-           align_up(S * arena_cap * 32) + align_up(S * impl_cap * 8);
+    return STATIC_ALIGN + align_up(S * 4) + align_up(S * (n_pad / 16) * 4) + align_up(S * n_pad * 4) +
+           align_up(S * m_pad * 4) + align_up(S * arena_cap * 32) + align_up(S * impl_cap * 8) +
+           align_up(S * impl_cap * 4);
 }
 
 }  // namespace
@@ -1395,12 +1538,19 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
         return set_error(GPSAT_ERR_STATE,
                          "gpsat_bcp_run_static: the formula is not on the device yet (gpsat_bcp_create on it "
                          "uploads it; this entry point allocates nothing, so it cannot upload)");
-    // switch devices only when needed: a caller capturing this call into a
-    // graph keeps its device current
+    // switch devices only when needed (a caller capturing this call into a
+    // graph keeps its device current), and back before returning
     int cur_dev = -1;
     cudaError_t err = cudaGetDevice(&cur_dev);
     if (err == cudaSuccess && cur_dev != f->device) err = cudaSetDevice(f->device);
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    struct Restore {
+        int dev, was;
+        ~Restore()
+        {
+            if (was >= 0 && was != dev) cudaSetDevice(was);
+        }
+    } restore{f->device, cur_dev};
     unsigned char *base = nullptr;
     int32_t resident = 0;
     int rc = static_setup(f->device, &base, &resident);
@@ -1420,8 +1570,8 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
         return set_error(GPSAT_ERR_CAPACITY, msg);
     }
     int64_t S = std::min<int64_t>(resident, std::max<int32_t>(n_trails, 1));
-    const int64_t per_slot = 4 + n_pad * 8 + m_pad * 4 + acap * 32 + impl_cap * 8;
-    S = std::min<int64_t>(S, std::max<int64_t>(1, (limit - 7 * STATIC_ALIGN) / per_slot));
+    const int64_t per_slot = 4 + (n_pad / 16) * 4 + n_pad * 4 + m_pad * 4 + acap * 32 + impl_cap * 12;
+    S = std::min<int64_t>(S, std::max<int64_t>(1, (limit - 9 * STATIC_ALIGN) / per_slot));
     while (S > 1 && static_layout_bytes(S, n_pad, m_pad, acap, impl_cap) > limit) S--;
 
     unsigned char *p = base;
@@ -1432,18 +1582,21 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     };
     unsigned int *counter = reinterpret_cast<unsigned int *>(take(STATIC_ALIGN));
     uint32_t *epoch = reinterpret_cast<uint32_t *>(take(S * 4));
-    bcp::VarRec *vr = reinterpret_cast<bcp::VarRec *>(take(S * n_pad * 8));
+    uint32_t *asg = reinterpret_cast<uint32_t *>(take(S * (n_pad / 16) * 4));
+    uint32_t *dh = reinterpret_cast<uint32_t *>(take(S * n_pad * 4));
     uint32_t *cst = reinterpret_cast<uint32_t *>(take(S * m_pad * 4));
     int4 *arena = reinterpret_cast<int4 *>(take(S * acap * 32));
     int2 *stack = reinterpret_cast<int2 *>(take(S * impl_cap * 8));
+    int32_t *impl = reinterpret_cast<int32_t *>(take(S * impl_cap * 4));
 
     cudaStream_t st = (cudaStream_t)stream;
     // what the kernel expects to find zero: the launch counter, the slots'
-    // epochs and their epoch-tagged state (a previous call may have used
-    // another formula with another layout)
+    // epochs, assignment words and epoch-tagged state (a previous call may
+    // have used another formula with another layout)
     err = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
     if (err == cudaSuccess) err = cudaMemsetAsync(epoch, 0, (size_t)S * 4, st);
-    if (err == cudaSuccess) err = cudaMemsetAsync(vr, 0, (size_t)(S * n_pad * 8), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(asg, 0, (size_t)(S * (n_pad / 16) * 4), st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(dh, 0, (size_t)(S * n_pad * 4), st);
     if (err == cudaSuccess) err = cudaMemsetAsync(cst, 0, (size_t)(S * m_pad * 4), st);
     if (err != cudaSuccess) return cuda_error(err, "gpsat_bcp_run_static: clearing the static scratch");
     if (n_trails == 0) return GPSAT_OK;
@@ -1454,13 +1607,16 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     d.lits = f->d_lits;
     d.w0off = f->d_w0off;
     d.w0ent = reinterpret_cast<const int4 *>(f->d_w0ent);
-    d.vr = vr;
+    d.asg = asg;
+    d.dh = dh;
     d.cst = cst;
     d.arena = arena;
     d.stack = stack;
+    d.impl = impl;
     d.epoch = epoch;
     d.next_trail = counter;
     d.order = nullptr;
+    d.n_words = n_pad / 16;
     d.n_pad = n_pad;
     d.m_pad = m_pad;
     d.arena_cap = acap;
@@ -1476,8 +1632,7 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     d.ilit = impl_lit;
     d.ireason = impl_reason;
     d.counters = counters;
-    const int blocks = (int)((S + bcp::WARPS - 1) / bcp::WARPS);
-    bcp::bcp_kernel<<<blocks, bcp::WARPS * 32, 0, st>>>(d);
+    bcp::bcp_kernel<<<(int)S, bcp::NT, 0, st>>>(d);
     err = cudaGetLastError();
     if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch (static scratch)");
     return GPSAT_OK;

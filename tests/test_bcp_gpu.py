@@ -74,11 +74,12 @@ def test_bcp_edge_cases(gpsat, orc, cuda_ok):
 
 
 def test_bcp_slot_reuse_and_epoch_wrap(gpsat, orc, cuda_ok):
-    # 2 slots serve 400 trails: every slot runs past its 127-trail epoch range
+    # one slot serves 400 trails: it runs past its 255-trail epoch range and
+    # wipes its list heads and clause states once
     n = 1000
     lits, off = gpsat.gen_random_ksat(12, n, 4200, 3)
     tl, to = gpsat.gen_trails(13, n, 400, 0.01, 0.10)
-    g, o = run_both(gpsat, orc, lits, off, n, tl, to, impl_cap=n, max_slots=2)
+    g, o = run_both(gpsat, orc, lits, off, n, tl, to, impl_cap=n, max_slots=1)
     compare_bcp(g, o, label="slot reuse")
 
 
