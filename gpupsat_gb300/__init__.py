@@ -41,7 +41,7 @@ class SolveOptions(ctypes.Structure):
                 ("learnt_first", ctypes.c_int32), ("learnt_inc", ctypes.c_int32), ("minimize", ctypes.c_int32),
                 ("conflict_budget", ctypes.c_int64), ("phase_init", ctypes.c_int32),
                 ("max_slots", ctypes.c_int32), ("log_participation", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("proof_words", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class GpsatError(RuntimeError):
@@ -88,6 +88,9 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_batch_solve": (ctypes.c_int, [_vp, ctypes.POINTER(SolveOptions), _vp, _vp, _vp, ctypes.c_int32]
                               + [_vp] * 5),
         "gpsat_check_model": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int32, _c_i64p]),
+        "gpsat_batch_proof": (ctypes.c_int, [_vp, ctypes.c_int32, _c_i32p, _vp, ctypes.c_int64, _c_i64p]),
+        "gpsat_check_rup": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32, _vp,
+                                           ctypes.c_int64, _c_i64p]),
         "gpsat_gen_random_ksat": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]),
         "gpsat_gen_trails": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                             ctypes.c_double, _vp, _vp]),
@@ -394,6 +397,20 @@ def check_model(lits: np.ndarray, offsets: np.ndarray, model: np.ndarray, n_vars
     return rc == 1
 
 
+def check_rup(lits: np.ndarray, offsets: np.ndarray, n_vars: int, proof: np.ndarray, assumptions=None) -> tuple:
+    """Host RUP check of an UNSAT proof log (gpsat_check_rup): (refuted, failed_step)."""
+    lits = np.ascontiguousarray(lits, np.int32)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    proof = np.ascontiguousarray(proof, np.int32)
+    a = None if assumptions is None or len(assumptions) == 0 else np.ascontiguousarray(assumptions, np.int32)
+    step = ctypes.c_int64(-1)
+    rc = lib().gpsat_check_rup(_p(lits), _p(offsets), len(offsets) - 1, n_vars, _p(a), 0 if a is None else len(a),
+                               _p(proof) if len(proof) else None, len(proof), ctypes.byref(step))
+    if rc < 0:
+        check(rc)
+    return rc == 1, step.value
+
+
 class Batch:
     """Many formulas solved on the GPU by the device CDCL solver (one warp per job)."""
 
@@ -438,17 +455,20 @@ class Batch:
         p = None if phase is None else np.ascontiguousarray(phase, np.int8)
         check(lib().gpsat_batch_set_seeds(self._h, _p(a), _p(p)))
 
-    def solve(self, options: SolveOptions | None = None, jobs=None, participation: bool | int = False) -> dict:
+    def solve(self, options: SolveOptions | None = None, jobs=None, participation: bool | int = False,
+              proof_words: int = 0) -> dict:
         """jobs: None, or (job_formula int32[J], cube_offsets int64[J+1], cube_lits int32[...]).
         participation: True / 1 logs per-variable conflict participation
         (out["participation"]); 2 also learnt-clause occurrences
         (out["learnt_occurrences"])."""
         F = self.n_formulas
         V = int(self.var_off[-1])
-        o = options or solve_options()
+        o = SolveOptions.from_buffer_copy(options) if options is not None else solve_options()
         level = int(participation)
         if level:
             o.log_participation = level
+        if proof_words:
+            o.proof_words = int(proof_words)
         out = dict(verdict=np.zeros(F, np.int32), model=np.zeros(V, np.int8),
                    stats=np.zeros((F, 9), np.int64), model_ok=np.zeros(F, np.int32),
                    participation=np.zeros(V * (2 if level >= 2 else 1), np.int32) if level else None)
@@ -465,6 +485,46 @@ class Batch:
         if level >= 2:
             out["learnt_occurrences"] = out["participation"][V:]
             out["participation"] = out["participation"][:V]
+        return out
+
+    def proof(self, job: int) -> tuple:
+        """(job verdict, proof log as int32 words, or None when it overflowed)
+        of a job of the last solve made with proof_words > 0 (gpsat_batch_proof)."""
+        v, n = ctypes.c_int32(), ctypes.c_int64()
+        check(lib().gpsat_batch_proof(self._h, job, ctypes.byref(v), None, 0, ctypes.byref(n)))
+        if n.value < 0:
+            return v.value, None
+        w = np.empty(max(n.value, 1), np.int32)
+        check(lib().gpsat_batch_proof(self._h, job, ctypes.byref(v), _p(w), n.value, ctypes.byref(n)))
+        return v.value, w[:n.value]
+
+    def certify_unsat(self, verdicts, jobs=None, threads: int | None = None) -> dict:
+        """Checks the proof log of every UNSAT job of the last solve (made with
+        proof_words > 0) against the original clauses and the job's cube, on
+        the host, several jobs at a time.  Returns {caller job: (ok, failed
+        step or reason)} for the jobs whose own verdict is UNSAT."""
+        import concurrent.futures as cf
+        if jobs is None:
+            todo = [(int(f), int(f), None) for f in np.nonzero(np.asarray(verdicts) == UNSAT)[0]]
+        else:
+            jf, co, cl = jobs
+            todo = [(j, int(jf[j]), cl[co[j]:co[j + 1]]) for j in range(len(jf))]
+
+        def one(item):
+            j, f, cube = item
+            v, words = self.proof(j)
+            if v != UNSAT:
+                return j, None
+            if words is None:
+                return j, (False, "log overflowed")
+            lits, off = self.formula(f)
+            return j, check_rup(lits, off, int(self.n_vars[f]), words, cube)
+
+        out = {}
+        with cf.ThreadPoolExecutor(threads or os.cpu_count() or 4) as ex:
+            for j, r in ex.map(one, todo):
+                if r is not None:
+                    out[j] = r
         return out
 
     def model_of(self, out: dict, f: int) -> np.ndarray:

@@ -122,6 +122,8 @@ struct Ctx {
     int32_t check;   // first failed consistency check (CheckCode), 0 if none
     int32_t why;     // which limit set `resource` (ResourceCode)
     int64_t conflicts, decisions, props, restarts, reduces, rebuilds;
+    int32_t *proof;  // this job's proof log (null: none)
+    int64_t plen;    // words logged, -1 once the log overflowed
 };
 
 __device__ __forceinline__ void fail_check(Ctx &C, int code)
@@ -1092,6 +1094,8 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
     C.check = 0;
     C.why = 0;
     C.conflicts = C.decisions = C.props = C.restarts = C.reduces = C.rebuilds = 0;
+    C.proof = P.proof ? P.proof + (size_t)job * (size_t)P.proof_cap : nullptr;
+    C.plen = 0;
     C.part = (P.part && o.log_participation) ? P.part + voff : nullptr;
     C.occ = (P.part && o.log_participation >= 2) ? P.part + P.var_total + voff : nullptr;
     for (int v = lane; v < C.n; v += 32) {
@@ -1183,6 +1187,16 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
             }
             if (C.occ)
                 for (int k = lane; k < len; k += 32) atomicAdd(&C.occ[C.learnt[k] >> 1], 1);
+            if (C.proof && C.plen >= 0) {
+                // the proof log: the learnt clause as derived, before it is stored
+                if (C.plen + 1 + len <= P.proof_cap) {
+                    if (lane == 0) C.proof[C.plen] = len;
+                    for (int k = lane; k < len; k += 32) C.proof[C.plen + 1 + k] = C.learnt[k];
+                    C.plen += 1 + len;
+                } else {
+                    C.plen = -1;
+                }
+            }
             backtrack(C, bt);
             int32_t r = -1;
             if (len >= 2) {
@@ -1262,6 +1276,7 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
             assign_lane0(C, d, -1, C.dlevel);
         }
     }
+    if (C.proof && lane == 0) P.proof_len[job] = C.plen;
     stats[ST_CONFLICTS] = C.conflicts;
     stats[ST_DECISIONS] = C.decisions;
     stats[ST_PROPS] = C.props;

@@ -70,6 +70,12 @@ struct Params {
     int32_t *part;               // per (instance, var): conflict participation (optional); with
                                  // log_participation 2 followed by learnt-clause occurrences
     int64_t var_total;           // variables of all instances (the second half's offset)
+    // optional proof log: job j appends each learnt clause as [len, literals...]
+    // (internal encoding) to proof[j * proof_cap ...]; proof_len[j] = words
+    // written, or -1 when the clauses outgrew proof_cap
+    int32_t *proof;
+    int64_t *proof_len;
+    int64_t proof_cap;
     // workspace
     int32_t n_slots;
     int32_t N;                   // max vars (padded to 16)

@@ -100,6 +100,12 @@ struct gpsat_batch {
     int32_t *d_job_verdict = nullptr;
     int64_t *d_job_stats = nullptr;
     int64_t job_cap = 0, cube_cap = 0;
+    // proof logs of the last solve (proof_words > 0): per job, and the
+    // caller's job index -> internal job (-1: no job, preprocessing decided it)
+    int32_t *d_proof = nullptr;
+    int64_t *d_proof_len = nullptr;
+    int64_t proof_words = 0, proof_bytes = 0, proof_len_cap = 0;
+    std::vector<int32_t> caller_job, job_verdict;
     unsigned int *d_counter = nullptr;
     // workspace
     cdcl::Params P{};
@@ -130,7 +136,8 @@ void batch_free(gpsat_batch *b)
     void *ptrs[] = {b->d_lits, b->d_cb, b->d_ce, b->d_nv, b->d_coff, b->d_var_off, b->d_olits, b->d_ocb,
                     b->d_oce, b->d_ocoff, b->d_model, b->d_state, b->d_verdict, b->d_ok, b->d_part,
                     b->d_seed_act, b->d_seed_phase, b->d_job_inst, b->d_job_cube_off, b->d_job_cube_len,
-                    b->d_cubes, b->d_job_verdict, b->d_job_stats, b->d_counter, b->ws};
+                    b->d_cubes, b->d_job_verdict, b->d_job_stats, b->d_counter, b->ws, b->d_proof,
+                    b->d_proof_len};
     for (void *p : ptrs) cudaFree(p);
 }
 
@@ -408,8 +415,13 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     // jobs: given, or one per formula; preprocessing-decided formulas get none.
     // A job's level-0 facts are the literals preprocessing fixed, then its cube.
     std::vector<int32_t> jinst, jcoff, jclen, cubes;
+    b->caller_job.clear();
     auto add_job = [&](int32_t f, const int32_t *cube, int64_t clen) {
-        if (b->prep[f].verdict != GPSAT_UNKNOWN) return;
+        if (b->prep[f].verdict != GPSAT_UNKNOWN) {
+            b->caller_job.push_back(-1);
+            return;
+        }
+        b->caller_job.push_back((int32_t)jinst.size());
         jinst.push_back(f);
         jcoff.push_back((int32_t)cubes.size());
         for (int32_t l : b->prep[f].solved) cubes.push_back(l);
@@ -456,6 +468,29 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (o.log_participation < 0 || o.log_participation > 2)
         return set_error(GPSAT_ERR_ARG, "log_participation must be 0, 1 or 2");
     const int64_t PV = o.log_participation >= 2 ? 2 * V : V;
+    // proof logs: proof_words per job
+    if (o.proof_words < 0) return set_error(GPSAT_ERR_ARG, "proof_words must be >= 0");
+    b->proof_words = o.proof_words;
+    if (o.proof_words > 0 && J > 0) {
+        const int64_t need = (int64_t)J * o.proof_words * 4;
+        if (need > b->proof_bytes) {
+            cudaFree(b->d_proof);
+            b->d_proof = nullptr;
+            b->proof_bytes = 0;
+            if (cudaMalloc(&b->d_proof, need) != cudaSuccess) {
+                cudaGetLastError();
+                return set_error(GPSAT_ERR_NOMEM, "proof log allocation");
+            }
+            b->proof_bytes = need;
+        }
+        if (J > b->proof_len_cap) {
+            cudaFree(b->d_proof_len);
+            b->d_proof_len = nullptr;
+            b->proof_len_cap = 0;
+            if (!dalloc(&b->d_proof_len, J)) return set_error(GPSAT_ERR_NOMEM, "proof lengths");
+            b->proof_len_cap = J;
+        }
+    }
     if (o.log_participation && b->part_cap < PV) {
         cudaFree(b->d_part);
         b->d_part = nullptr;
@@ -477,6 +512,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
          cudaMemsetAsync(b->d_model, 0, V, st) == cudaSuccess &&
          cudaMemsetAsync(b->d_counter, 0, 4, st) == cudaSuccess;
     if (ok && o.log_participation) ok = cudaMemsetAsync(b->d_part, 0, PV * 4, st) == cudaSuccess;
+    if (ok && o.proof_words > 0 && J > 0) ok = cudaMemsetAsync(b->d_proof_len, 0, (size_t)J * 8, st) == cudaSuccess;
     if (!ok) return cuda_error(cudaGetLastError(), "solve setup");
     cdcl::Params &P = b->P;
     P.o.decide = o.decide;
@@ -511,6 +547,9 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     P.model = b->d_model;
     P.part = o.log_participation ? b->d_part : nullptr;
     P.var_total = V;
+    P.proof = o.proof_words > 0 ? b->d_proof : nullptr;
+    P.proof_len = o.proof_words > 0 ? b->d_proof_len : nullptr;
+    P.proof_cap = o.proof_words;
     if (J) {
         const int slots = std::min<int32_t>(b->ws_slots, J);
         P.n_slots = slots;
@@ -537,6 +576,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     if (!ok) return cuda_error(cudaGetLastError(), "result copy");
     err = cudaStreamSynchronize(st);
     if (err != cudaSuccess) return cuda_error(err, "solve");
+    b->job_verdict = jv;
     std::vector<int32_t> n_unsat(F, 0), n_jobs_f(F, 0);
     if (stats) std::memset(stats, 0, sizeof(int64_t) * (size_t)F * GPSAT_SOLVE_NSTATS);
     for (int32_t j = 0; j < J; j++) {
@@ -598,6 +638,40 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         // eliminated variables: the solver never wrote them
         for (int32_t f = 0; f < F; f++)
             if (vd[f] == GPSAT_SAT) pad_model(models + b->var_off[f], b->n_vars[f]);
+    }
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_batch_proof(const gpsat_batch *b, int32_t job, int32_t *verdict, int32_t *words, int64_t cap,
+                                 int64_t *len)
+{
+    if (!b || !len || cap < 0 || (cap > 0 && !words)) return set_error(GPSAT_ERR_ARG, "gpsat_batch_proof: bad argument");
+    if (job < 0 || job >= (int32_t)b->caller_job.size())
+        return set_error(GPSAT_ERR_ARG, "gpsat_batch_proof: job outside the last solve's jobs");
+    const int32_t j = b->caller_job[job];
+    *len = 0;
+    if (j < 0) {   // decided by preprocessing: no search, nothing logged
+        if (verdict) *verdict = GPSAT_UNKNOWN;
+        return GPSAT_OK;
+    }
+    if (verdict) *verdict = b->job_verdict[j];
+    if (b->proof_words <= 0) return GPSAT_OK;
+    cudaError_t err = cudaSetDevice(b->device);
+    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    int64_t n = 0;
+    if (cudaMemcpy(&n, b->d_proof_len + j, 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return cuda_error(cudaGetLastError(), "proof length copy");
+    *len = n;
+    if (n <= 0 || cap <= 0) return GPSAT_OK;
+    const int64_t k = std::min(n, cap);
+    if (cudaMemcpy(words, b->d_proof + (size_t)j * (size_t)b->proof_words, (size_t)k * 4, cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+        return cuda_error(cudaGetLastError(), "proof copy");
+    // literals to DIMACS, lengths as they are
+    for (int64_t p = 0; p < k;) {
+        const int64_t l = words[p];
+        for (int64_t i = 1; i <= l && p + i < k; i++) words[p + i] = dimacs_of_lit(words[p + i]);
+        p += 1 + l;
     }
     return GPSAT_OK;
 }

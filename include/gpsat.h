@@ -196,7 +196,9 @@ typedef struct {
     int32_t max_slots;         /* jobs in flight (0 = as many as the GPU keeps resident) */
     int32_t log_participation; /* 1: count, per variable, the conflicts whose analysis saw it;
                                   2: also its occurrences in learnt clauses */
-    int32_t reserved[5];
+    int32_t proof_words;       /* > 0: every job logs its learnt clauses, in the order learnt,
+                                  in a log of this many int32 words (see gpsat_batch_proof) */
+    int32_t reserved[4];
 } gpsat_solve_options;
 
 /* per-formula statistics written by gpsat_batch_solve (summed over its jobs) */
@@ -233,6 +235,28 @@ int gpsat_batch_set_seeds(gpsat_batch *b, const float *activity, const int8_t *p
 int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt, const int32_t *job_formula,
                       const int64_t *cube_offsets, const int32_t *cube_lits, int32_t n_jobs, int32_t *verdicts,
                       int8_t *models, int64_t *stats, int32_t *model_ok, int32_t *participation);
+/* The proof log of one job of the last gpsat_batch_solve made with
+ * proof_words > 0 (no counterpart in the reference, which outputs no proof).
+ * job is the caller's job index (the formula index when the solve was given no
+ * job list).  The log is the job's learnt clauses in the order learnt, each as
+ * [length, DIMACS literal...]; up to cap words are copied to words.  *len is the
+ * log's size in words, 0 when nothing was logged (no search ran, or logging was
+ * off) and -1 when the clauses outgrew proof_words (the log is then incomplete).
+ * *verdict (may be NULL) is the job's own verdict.  A job's UNSAT is certified
+ * by gpsat_check_rup over the original clauses, the job's cube and this log. */
+int gpsat_batch_proof(const gpsat_batch *b, int32_t job, int32_t *verdict, int32_t *words, int64_t cap,
+                      int64_t *len);
+/* Host checker of UNSAT proofs by reverse unit propagation, independent of the
+ * device solver (no counterpart in the reference): returns 1 when the formula
+ * (clauses in CSR, DIMACS) with the assumption literals is refuted -- every
+ * clause of the proof log ([length, literal...] per clause) follows from
+ * everything before it by unit propagation, and unit propagation over the
+ * formula, the assumptions and the log ends in a conflict -- 0 when a step
+ * fails (*failed_step = its index, or the number of steps when the log ends
+ * without a conflict), negative on bad input. */
+int gpsat_check_rup(const int32_t *lits, const int64_t *offsets, int64_t n_clauses, int32_t n_vars,
+                    const int32_t *assumptions, int32_t n_assumptions, const int32_t *proof, int64_t proof_len,
+                    int64_t *failed_step);
 /* Independent host model check: 1 if every clause holds a true literal, 0 if
  * not (first_false_clause set), negative on bad input.
  * (the reference's own "verified" check, SATSolver/Results.cu:143-155,
