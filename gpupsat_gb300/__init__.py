@@ -19,6 +19,7 @@ LIB_PATH = _PKG / "libgpsat.so"
 OK = 0
 UNKNOWN, SAT, UNSAT = 0, 10, 20
 BCP_NO_CONFLICT, BCP_CONFLICT, BCP_OVERFLOW, BCP_BAD_TRAIL = 0, 1, -1, -2
+BCP_WATCHED, BCP_FULL_SCAN = 0, 1
 BCP_NCOUNTERS = 6
 BCP_COUNTER_NAMES = ("props", "watches", "clause_lits", "lookups", "implications", "trail_lits")
 
@@ -76,6 +77,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_bcp_destroy": (ctypes.c_int, [_vp]),
         "gpsat_bcp_info": (ctypes.c_int, [_vp, _c_i32p, _c_i64p]),
         "gpsat_bcp_set_active_slots": (ctypes.c_int, [_vp, ctypes.c_int32]),
+        "gpsat_bcp_set_strategy": (ctypes.c_int, [_vp, ctypes.c_int32]),
         "gpsat_bcp_run_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 8),
         "gpsat_bcp_run_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 7),
         "gpsat_bcp_run_static": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp, ctypes.c_int32]
@@ -262,6 +264,13 @@ class BCPBatch:
         s, b = ctypes.c_int32(), ctypes.c_int64()
         check(lib().gpsat_bcp_info(self._h, ctypes.byref(s), ctypes.byref(b)))
         return dict(slots=s.value, device_bytes=b.value)
+
+    def set_strategy(self, strategy: str) -> None:
+        """"watched" (two watched literals, the default) or "full_scan" (the
+        reference's full-scan clause evaluation) for the runs that follow."""
+        code = {"watched": BCP_WATCHED, "full_scan": BCP_FULL_SCAN}.get(strategy, -1)
+        check(lib().gpsat_bcp_set_strategy(self._h, code))
+        self.strategy = strategy
 
     def set_active_slots(self, n: int) -> None:
         """Later runs use at most n slots (0 = all); outputs do not depend on it."""

@@ -1087,6 +1087,220 @@ __global__ void order_scatter(const int64_t *toff, int T, unsigned *hist, int32_
         order[atomicAdd(&hist[order_bucket(toff, t)], 1u)] = t;
 }
 
+// ---------------------------------------------------------------------------
+// Full-scan clause evaluation: the reference's BASIC_SEARCH strategy
+// (ConflictAnalysis/ConflictAnalyzer.cu:173-245, clause_status :298-313 and
+// SATSolver/VariablesStateHandler.cu:180-206).  Every trail literal is
+// assigned, then sweeps run over all clauses in index order; a clause with a
+// true literal is satisfied, one with every literal false is a conflict (the
+// trail stops there), one with a single unassigned literal and the rest false
+// implies it at once, so the clauses after it see the implication; sweeps
+// repeat while one adds implications.
+//
+// One thread block per trail.  A pass evaluates the next SCAN_NT * SCAN_PER
+// clauses at once against the current assignment; the first clause (lowest
+// index) that is unit or false -- a block-wide minimum -- is the next event
+// of the sequential sweep: the clauses before it are final, an implication is
+// committed and the rest of the pass is evaluated again.  The trail's
+// assignment bits sit in shared memory when they fit (SCAN_SMEM_WORDS), else
+// in the slot's assignment words.  Counters: [0] sweeps, [1] clause
+// evaluations, [2] and [3] literals examined, [4] implications, [5] trail
+// literals; stop_index is the sweep (0-based) that met the conflict.
+constexpr int SCAN_NT = 256;
+constexpr int SCAN_PER = 4;
+constexpr int SCAN_SPAN = SCAN_NT * SCAN_PER;
+constexpr int64_t SCAN_SMEM_WORDS = 12288;   // 48 KB: formulas up to 196,608 variables
+
+template <bool SMEM>
+__global__ void __launch_bounds__(SCAN_NT) scan_kernel(Dev d, const uint32_t *__restrict__ coff)
+{
+    extern __shared__ uint32_t sasg[];
+    __shared__ int s_key[3];   // per pass, in rotation: a slot is reset two barriers before its next use
+    __shared__ int s_t;
+    __shared__ unsigned long long s_red[SCAN_NT / 32][3];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int slot = blockIdx.x;
+    if (slot >= d.n_slots) return;
+    const int32_t n = d.n_vars;
+    const int64_t m = d.n_clauses;
+    uint32_t *asg = SMEM ? sasg : d.asg + (size_t)slot * d.n_words;
+    while (true) {
+        if (tid == 0) s_t = (int)atomicAdd(d.next_trail, 1u);
+        __syncthreads();
+        const int t0 = s_t;
+        if (t0 >= d.n_trails) break;
+        const int t = d.order ? d.order[t0] : t0;
+        if (SMEM)
+            for (int64_t i = tid; i < d.n_words; i += SCAN_NT) sasg[i] = 0u;
+        __syncthreads();
+        const int64_t tb = d.toff[t], tn = d.toff[t + 1] - tb;
+        int32_t *ilit = d.ilit + (size_t)t * d.impl_cap;
+        int32_t *ireason = d.ireason + (size_t)t * d.impl_cap;
+        bool bad = tn < 0;
+        for (int64_t i = tid; i < tn; i += SCAN_NT) {
+            const int32_t x = d.trail[tb + i];
+            if (x == 0 || x > n || x < -n) {
+                bad = true;
+            } else {
+                const int32_t v = (x > 0 ? x : -x) - 1;
+                const int sh = (v & 15) << 1;
+                const uint32_t bits = (x > 0 ? 3u : 1u) << sh;
+                const uint32_t old = atomicOr(&asg[v >> 4], bits);
+                if (((old >> sh) & 1u) && (((old ^ bits) >> sh) & 2u)) bad = true;
+            }
+        }
+        bad = __syncthreads_or(bad);
+        int32_t status = bad ? GPSAT_BCP_BAD_TRAIL : GPSAT_BCP_NO_CONFLICT, confl = -1, stopi = -1;
+        int64_t n_impl = 0, last = -1, sweeps = 0;
+        int64_t myW = 0, myL = 0;
+        int kb = 0;
+        if (tid == 0) s_key[0] = s_key[1] = s_key[2] = INT_MAX;
+        __syncthreads();
+        while (status == GPSAT_BCP_NO_CONFLICT && last != n_impl) {
+            last = n_impl;
+            const int64_t sweep = sweeps++;
+            for (int64_t base = 0; base < m && status == GPSAT_BCP_NO_CONFLICT; base += SCAN_SPAN) {
+                int64_t cursor = base;
+                const int64_t end = base + SCAN_SPAN < m ? base + SCAN_SPAN : m;
+                while (cursor < end) {
+                    // evaluate this thread's clauses of [cursor, end)
+                    int ev_key = INT_MAX;
+                    int32_t unit[SCAN_PER];
+                    int exam[SCAN_PER];
+                    bool fals[SCAN_PER];
+#pragma unroll
+                    for (int j = 0; j < SCAN_PER; j++) {
+                        const int64_t c = base + tid + (int64_t)j * SCAN_NT;
+                        unit[j] = -1;
+                        exam[j] = 0;
+                        fals[j] = false;
+                        if (c >= cursor && c < end) {
+                            const uint32_t b = coff[c], e = coff[c + 1];
+                            int unsat = 0, k = 0;
+                            int32_t learnt = -1;
+                            bool sat = false;
+                            for (uint32_t i = b; i < e; i++) {
+                                const int32_t l = d.lits[i];
+                                const uint32_t bits = asg_bits(asg[(l >> 1) >> 4], l >> 1);
+                                k++;
+                                if (!(bits & 1u)) learnt = l;
+                                else if ((bits >> 1) == (uint32_t)(l & 1)) {
+                                    sat = true;
+                                    break;
+                                } else unsat++;
+                            }
+                            exam[j] = k;
+                            const int len = (int)(e - b);
+                            if (!sat && unsat == len) {
+                                fals[j] = true;
+                                ev_key = min(ev_key, (int)(c - base));
+                            } else if (!sat && unsat == len - 1) {
+                                unit[j] = learnt;
+                                ev_key = min(ev_key, (int)(c - base));
+                            }
+                        }
+                    }
+                    ev_key = __reduce_min_sync(FULL, ev_key);
+                    if (lane == 0 && ev_key != INT_MAX) atomicMin(&s_key[kb], ev_key);
+                    __syncthreads();
+                    const int key = s_key[kb];
+                    if (tid == 0) s_key[kb == 0 ? 2 : kb - 1] = INT_MAX;   // the slot after next
+                    kb = kb == 2 ? 0 : kb + 1;
+                    const int64_t upto = key == INT_MAX ? end : base + key + 1;   // clauses final after this pass
+#pragma unroll
+                    for (int j = 0; j < SCAN_PER; j++) {
+                        const int64_t c = base + tid + (int64_t)j * SCAN_NT;
+                        if (c >= cursor && c < upto) {
+                            myW++;
+                            myL += exam[j];
+                        }
+                    }
+                    if (key == INT_MAX) break;
+                    const int64_t c = base + key;
+                    const int j = (int)((c - base) / SCAN_NT);
+                    const bool mine = (int)((c - base) % SCAN_NT) == tid;
+                    // the event's kind: the owner tells everyone
+                    int kind = 0;   // 1 conflict, 2 implication
+                    if (mine) {
+                        int32_t u = -1;
+                        bool f = false;
+#pragma unroll
+                        for (int q = 0; q < SCAN_PER; q++)
+                            if (q == j) {
+                                u = unit[q];
+                                f = fals[q];
+                            }
+                        kind = f ? 1 : 2;
+                        if (!f && n_impl < d.impl_cap) {
+                            ilit[n_impl] = dimacs_of(u);
+                            ireason[n_impl] = (int32_t)c;
+                            const int32_t v = u >> 1;
+                            atomicOr(&asg[v >> 4], ((u & 1) ? 3u : 1u) << ((v & 15) << 1));
+                        }
+                        s_red[0][0] = (unsigned long long)kind;
+                    }
+                    __syncthreads();
+                    kind = (int)s_red[0][0];
+                    __syncthreads();
+                    if (kind == 1) {
+                        confl = (int32_t)c;
+                        stopi = (int32_t)sweep;
+                        status = GPSAT_BCP_CONFLICT;
+                        break;
+                    }
+                    if (n_impl >= d.impl_cap) {
+                        stopi = (int32_t)sweep;
+                        status = GPSAT_BCP_OVERFLOW;
+                        break;
+                    }
+                    n_impl++;
+                    cursor = c + 1;
+                }
+            }
+        }
+        // clear what this trail set in the slot's assignment words
+        if (!SMEM) {
+            for (int64_t i = tid; i < tn; i += SCAN_NT) {
+                const int32_t x = d.trail[tb + i];
+                if (x != 0 && x <= n && x >= -n) asg[((x > 0 ? x : -x) - 1) >> 4] = 0u;
+            }
+            __syncthreads();   // implied literals are read back from the outputs
+            for (int64_t i = tid; i < n_impl; i += SCAN_NT) {
+                const int32_t x = ilit[i];
+                asg[((x > 0 ? x : -x) - 1) >> 4] = 0u;
+            }
+        }
+        myW = warp_sum(myW);
+        myL = warp_sum(myL);
+        if (lane == 0) {
+            s_red[wid][1] = (unsigned long long)myW;
+            s_red[wid][2] = (unsigned long long)myL;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int64_t W_ = 0, L_ = 0;
+            for (int w = 0; w < SCAN_NT / 32; w++) {
+                W_ += (int64_t)s_red[w][1];
+                L_ += (int64_t)s_red[w][2];
+            }
+            d.status[t] = status;
+            d.conflict[t] = confl;
+            d.stop[t] = stopi;
+            d.nimpl[t] = n_impl;
+            if (d.counters) {
+                int64_t *cn = d.counters + (size_t)t * GPSAT_BCP_NCOUNTERS;
+                cn[0] = bad ? 0 : sweeps;
+                cn[1] = W_;
+                cn[2] = L_;
+                cn[3] = L_;
+                cn[4] = n_impl;
+                cn[5] = bad ? 0 : tn;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // blocks per SM the register allocation targets
 #ifndef GPSAT_BCP_MIN_BLOCKS
 #define GPSAT_BCP_MIN_BLOCKS 4
@@ -1120,6 +1334,8 @@ struct gpsat_bcp {
     int device = 0;
     int32_t slots = 0;
     int32_t active = 0;                // slots the launches use (0: all)
+    int32_t strategy = GPSAT_BCP_WATCHED;
+    int32_t scan_resident = 0;         // resident blocks of the full-scan kernel
     int64_t n_words = 0, n_pad = 0, m_pad = 0, arena_cap = 0, impl_cap = 0;
     uint32_t *asg = nullptr, *dh = nullptr, *cst = nullptr, *epoch = nullptr;
     int4 *arena = nullptr;
@@ -1216,7 +1432,19 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
         bcp::order_scatter<<<g, 256, 0, st>>>(toff, n_trails, b->hist, b->order);
         d.order = b->order;
     }
-    bcp::bcp_kernel<<<d.n_slots, bcp::NT, 0, st>>>(d);
+    if (b->strategy == GPSAT_BCP_FULL_SCAN) {
+        // one block per trail; the assignment bits in shared memory when they fit
+        const bool smem = b->n_words <= bcp::SCAN_SMEM_WORDS;
+        d.n_slots = std::min<int32_t>(smem ? b->scan_resident : std::min(b->scan_resident, b->slots),
+                                      std::max<int32_t>(n_trails, 1));
+        if (b->active > 0) d.n_slots = std::min(d.n_slots, b->active);
+        if (smem)
+            bcp::scan_kernel<true><<<d.n_slots, bcp::SCAN_NT, (size_t)b->n_words * 4, st>>>(d, f->d_coff);
+        else
+            bcp::scan_kernel<false><<<d.n_slots, bcp::SCAN_NT, 0, st>>>(d, f->d_coff);
+    } else {
+        bcp::bcp_kernel<<<d.n_slots, bcp::NT, 0, st>>>(d);
+    }
     err = cudaGetLastError();
     if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch");
     return GPSAT_OK;
@@ -1276,6 +1504,17 @@ extern "C" int gpsat_bcp_create(const gpsat_formula *f, int32_t max_slots, int64
         return set_error(GPSAT_ERR_NOMEM, "gpsat_bcp_create: device allocation failed");
     }
     b->bytes = (int64_t)S * per_slot;
+    {
+        int ps = 0;
+        const bool smem = b->n_words <= bcp::SCAN_SMEM_WORDS;
+        if (smem)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, bcp::scan_kernel<true>, bcp::SCAN_NT,
+                                                          (size_t)b->n_words * 4);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, bcp::scan_kernel<false>, bcp::SCAN_NT, 0);
+        cudaGetLastError();
+        b->scan_resident = std::max(1, sms * std::max(ps, 1));
+    }
     *out = b;
     return GPSAT_OK;
 }
@@ -1302,6 +1541,15 @@ extern "C" int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n)
     if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
     if (n < 0 || n > b->slots) return set_error(GPSAT_ERR_ARG, "gpsat_bcp_set_active_slots: n outside 0..slots");
     b->active = n;
+    return GPSAT_OK;
+}
+
+extern "C" int gpsat_bcp_set_strategy(gpsat_bcp *b, int32_t strategy)
+{
+    if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
+    if (strategy != GPSAT_BCP_WATCHED && strategy != GPSAT_BCP_FULL_SCAN)
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_set_strategy: unknown strategy");
+    b->strategy = strategy;
     return GPSAT_OK;
 }
 

@@ -142,6 +142,25 @@ int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
  * with equal ones all slots can (no counterpart in the reference). */
 int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n);
 
+/* The propagation strategy of the runs that follow (the reference chooses it at
+ * compile time, SATSolver/Configs.cuh:27-33, CONFLICT_ANALYSIS_STRATEGY):
+ *   GPSAT_BCP_WATCHED    two watched literals in the reference's order (default;
+ *                        reference TWO_WATCHED_LITERALS, BCPStrategy/WatchedClausesList.cu)
+ *   GPSAT_BCP_FULL_SCAN  full-scan clause evaluation (reference BASIC_SEARCH,
+ *                        ConflictAnalysis/ConflictAnalyzer.cu:173-245): every trail
+ *                        literal assigned, then sweeps over all clauses in index
+ *                        order, a unit clause implying at once, until a conflict or
+ *                        a sweep that implies nothing.  Outputs as above, except:
+ *                        stop_index = the sweep (0-based) that met the conflict;
+ *                        counters [0] sweeps, [1] clause evaluations, [2] and [3]
+ *                        literals examined, [4] implications, [5] trail literals.
+ * Trails run one per thread block; a formula of up to 196,608 variables keeps a
+ * trail's assignment in shared memory.  gpsat_bcp_run_static always runs
+ * GPSAT_BCP_WATCHED. */
+#define GPSAT_BCP_WATCHED 0
+#define GPSAT_BCP_FULL_SCAN 1
+int gpsat_bcp_set_strategy(gpsat_bcp *b, int32_t strategy);
+
 /* Allocation-free BCP (no counterpart in the reference, whose BCP allocates
  * its watch-node pool and graph up front): the same kernel and outputs as
  * gpsat_bcp_run_device, but the per-trail state lives in one fixed 64 MiB

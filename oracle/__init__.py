@@ -49,6 +49,7 @@ def lib() -> ctypes.CDLL:
         L.orc_bcp_destroy.argtypes = [_vp]
         L.orc_bcp_initial_watches.argtypes = [_vp, _vp, _vp]
         L.orc_bcp_run.argtypes = [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64] + [_vp] * 7
+        L.orc_scan_run.argtypes = [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64] + [_vp] * 7
         L.orc_gen_random_ksat.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp]
         L.orc_gen_trails.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                      ctypes.c_double, _vp, _vp]
@@ -96,14 +97,18 @@ class BCPOracle:
         lib().orc_bcp_initial_watches(self._h, _p(w1), _p(w2))
         return w1, w2
 
-    def run(self, trail_lits: np.ndarray, trail_offsets: np.ndarray, impl_cap: int = 4096, threads: int = 1) -> dict:
+    def run(self, trail_lits: np.ndarray, trail_offsets: np.ndarray, impl_cap: int = 4096, threads: int = 1,
+            strategy: str = "watched") -> dict:
+        """strategy "watched": the reference's two-watched-literal BCP;
+        "full_scan": its full-scan clause evaluation (BASIC_SEARCH)."""
         trail_lits = np.ascontiguousarray(trail_lits, dtype=np.int32)
         trail_offsets = np.ascontiguousarray(trail_offsets, dtype=np.int64)
         T = len(trail_offsets) - 1
         out = dict(status=np.empty(T, np.int32), conflict=np.empty(T, np.int32), stop=np.empty(T, np.int32),
                    n_impl=np.empty(T, np.int64), impl_lit=np.zeros((T, impl_cap), np.int32),
                    impl_reason=np.zeros((T, impl_cap), np.int32), counters=np.zeros((T, 6), np.int64))
-        rc = lib().orc_bcp_run(self._h, _p(trail_lits), _p(trail_offsets), T, threads, impl_cap,
+        fn = lib().orc_scan_run if strategy == "full_scan" else lib().orc_bcp_run
+        rc = fn(self._h, _p(trail_lits), _p(trail_offsets), T, threads, impl_cap,
                                _p(out["status"]), _p(out["conflict"]), _p(out["stop"]), _p(out["n_impl"]),
                                _p(out["impl_lit"]), _p(out["impl_reason"]), _p(out["counters"]))
         if rc != 0:

@@ -377,6 +377,68 @@ static int run_trail(const orc_bcp *f, orc_ws *w, const int32_t *tl, int64_t tn,
     return status;
 }
 
+/* ------------------------------------------------------------------ */
+/* Full-scan clause evaluation (the reference's BASIC_SEARCH strategy):
+ * every trail literal assigned, then sweeps over all clauses in index order,
+ * each clause evaluated by clause_status -- true literal: satisfied; all
+ * false: conflict, stop; exactly one unassigned (the last unassigned literal
+ * it met) and the rest false: implied at once, visible to the clauses after
+ * it -- repeated while a sweep adds implications.
+ *     ConflictAnalysis/ConflictAnalyzer.cu:173-245 (propagate_all_clauses),
+ *     :298-313 (clause_status), SATSolver/VariablesStateHandler.cu:180-206
+ * Counters: [0] sweeps, [1] clause evaluations, [2] literals examined,
+ * [3] assignment lookups (one per literal examined), [4] implications,
+ * [5] trail literals.  stop_index = the sweep (0-based) that met the conflict. */
+static int scan_trail(const orc_bcp *f, int8_t *val, const int32_t *tl, int64_t tn, orc_out *o,
+                      int32_t *conflict_clause, int32_t *stop_index)
+{
+    int64_t assigned = 0;
+    int status = ORC_BCP_NO_CONFLICT;
+    *conflict_clause = -1; *stop_index = -1;
+    for (int64_t i = 0; i < tn; i++) {
+        int32_t l = tl[i];
+        int8_t want = (l & 1) ? 1 : 2;
+        if (val[l >> 1] != 0 && val[l >> 1] != want) { status = ORC_BCP_BAD_TRAIL; break; }
+        val[l >> 1] = want;
+        assigned++;
+    }
+    int64_t last = -1, sweep = 0;
+    while (status == ORC_BCP_NO_CONFLICT && last != o->n_impl) {
+        last = o->n_impl;
+        o->props++;
+        for (int64_t c = 0; c < f->n_clauses && status == ORC_BCP_NO_CONFLICT; c++) {
+            int64_t b = f->coff[c], k = f->coff[c + 1] - b;
+            int64_t unsat = 0;
+            int32_t learnt = -1;
+            int sat = 0;
+            o->W++;
+            for (int64_t i = 0; i < k; i++) {
+                int32_t l = f->lits[b + i];
+                int8_t a = val[l >> 1];
+                o->L++; o->A++;
+                if (a == 0) learnt = l;
+                else if (a == ((l & 1) ? 1 : 2)) { sat = 1; break; }
+                else unsat++;
+            }
+            if (sat) continue;
+            if (unsat == k) {
+                *conflict_clause = (int32_t)c;
+                *stop_index = (int32_t)sweep;
+                status = ORC_BCP_CONFLICT;
+            } else if (unsat == k - 1) {
+                if (o->n_impl >= o->cap) { status = ORC_BCP_OVERFLOW; *stop_index = (int32_t)sweep; break; }
+                o->ilit[o->n_impl] = learnt; o->ireason[o->n_impl] = (int32_t)c; o->n_impl++;
+                val[learnt >> 1] = (learnt & 1) ? 1 : 2;
+                o->I++;
+            }
+        }
+        sweep++;
+    }
+    for (int64_t i = 0; i < assigned; i++) val[tl[i] >> 1] = 0;
+    for (int64_t i = 0; i < o->n_impl; i++) val[o->ilit[i] >> 1] = 0;
+    return status;
+}
+
 typedef struct {
     const orc_bcp *f;
     const int32_t *trail; const int64_t *toff;
@@ -386,6 +448,7 @@ typedef struct {
     int64_t *n_impl; int32_t *impl_lit, *impl_reason;
     int64_t *counters;
     int err;
+    int scan;          /* 1: full-scan clause evaluation instead of BCP */
 } orc_job;
 
 static void *worker(void *arg)
@@ -410,7 +473,8 @@ static void *worker(void *arg)
         o.ilit = j->impl_lit + (int64_t)t * j->impl_cap;
         o.ireason = j->impl_reason + (int64_t)t * j->impl_cap;
         int32_t cc = -1, si = -1;
-        int st = bad ? ORC_BCP_BAD_TRAIL : run_trail(f, &w, tl, tn, &o, &cc, &si);
+        int st = bad ? ORC_BCP_BAD_TRAIL
+                     : (j->scan ? scan_trail(f, w.val, tl, tn, &o, &cc, &si) : run_trail(f, &w, tl, tn, &o, &cc, &si));
         j->status[t] = st;
         j->conflict_clause[t] = cc;
         j->stop_index[t] = si;
@@ -435,10 +499,34 @@ static void *worker(void *arg)
  *   impl_lit[t*cap ..] (DIMACS signed) and impl_reason[t*cap ..] (clause index)
  *   counters[t*6 ..]   props, watch entries, clause literals, assignment
  *                      lookups, implications, trail literals assigned   */
+static int run_jobs(const orc_bcp *f, const int32_t *trail, const int64_t *toff, int32_t n_trails,
+                    int32_t n_threads, int64_t impl_cap, int scan,
+                    int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                    int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters);
+
 int orc_bcp_run(const orc_bcp *f, const int32_t *trail, const int64_t *toff, int32_t n_trails,
                 int32_t n_threads, int64_t impl_cap,
                 int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
                 int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
+{
+    return run_jobs(f, trail, toff, n_trails, n_threads, impl_cap, 0, status, conflict_clause, stop_index,
+                    n_impl, impl_lit, impl_reason, counters);
+}
+
+/* The same outputs for the full-scan strategy (scan_trail above). */
+int orc_scan_run(const orc_bcp *f, const int32_t *trail, const int64_t *toff, int32_t n_trails,
+                 int32_t n_threads, int64_t impl_cap,
+                 int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                 int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
+{
+    return run_jobs(f, trail, toff, n_trails, n_threads, impl_cap, 1, status, conflict_clause, stop_index,
+                    n_impl, impl_lit, impl_reason, counters);
+}
+
+static int run_jobs(const orc_bcp *f, const int32_t *trail, const int64_t *toff, int32_t n_trails,
+                    int32_t n_threads, int64_t impl_cap, int scan,
+                    int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                    int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
 {
     if (!f || n_trails < 0 || impl_cap < 0) return ORC_ERR_ARG;
     if (n_threads < 1) n_threads = 1;
@@ -453,6 +541,7 @@ int orc_bcp_run(const orc_bcp *f, const int32_t *trail, const int64_t *toff, int
         j->status = status; j->conflict_clause = conflict_clause; j->stop_index = stop_index;
         j->n_impl = n_impl; j->impl_lit = impl_lit; j->impl_reason = impl_reason;
         j->counters = counters;
+        j->scan = scan;
     }
     if (n_threads == 1) {
         worker(&jobs[0]);

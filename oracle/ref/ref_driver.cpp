@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "BCPStrategy/WatchedClausesList.cuh"
+#include "ConflictAnalysis/ConflictAnalyzer.cuh"
 #include "FileManager/FormulaData.cuh"
 #include "JobsManager/VariableChooser.cuh"
 #include "SATSolver/SATSolver.cuh"
@@ -203,6 +204,73 @@ int ref_rank_vars(const int32_t *lits, const int64_t *off, int32_t n_vars, int64
         k++;
     }
     return k;
+}
+
+namespace {
+// The reference's full-scan clause evaluation (BASIC_SEARCH) is a protected
+// member; a subclass calls it as the reference's own propagate() does.
+struct FullScan : public ConflictAnalyzer {
+    using ConflictAnalyzer::ConflictAnalyzer;
+    sat_status sweep(Decision d, const Clause **confl) { return propagate_all_clauses(d, confl); }
+};
+}  // namespace
+
+/* The reference's full-scan clause evaluation over a trail: every trail
+ * literal assigned as ref_bcp does, then ConflictAnalyzer::propagate_all_clauses
+ * (ConflictAnalysis/ConflictAnalyzer.cu:173-245).  Returns 0 (no conflict),
+ * 1 (conflict, *conflict_clause set), -2 (a variable given both signs), -3
+ * (preprocessing decided the formula), -1 (implication capacity); the implied
+ * literals in the order the sweeps found them. */
+int ref_scan(const int32_t *lits, const int64_t *off, int32_t n_vars, int64_t n_clauses, const int32_t *trail,
+             int64_t trail_len, int64_t cap, int32_t *impl_lit, int64_t *n_impl, int32_t *conflict_clause)
+{
+    *n_impl = 0;
+    *conflict_clause = -1;
+    FormulaData *fd = make_formula(lits, off, n_vars, n_clauses);
+    if (fd->get_status_after_preprocessing() != sat_status::UNDEF) return -3;
+    CUDAClauseVec formula = fd->get_formula_dev();
+    std::unordered_map<const Lit *, int32_t> index;
+    for (int i = 0; i < formula.size_of(); i++) index[formula.get_ptr(i)->literals] = i;
+    std::vector<Var> dead;
+    for (Lit l : fd->get_solved_literals()) dead.push_back(var(l));
+    GPUVecView<Var> dead_view(dead.data(), dead.size(), dead.size());
+    std::vector<Var> fv(n_vars);
+    std::vector<Decision> dec(n_vars + trail_len), imp(n_vars);
+    auto *handler = new VariablesStateHandler(n_vars, &dead_view, nullptr, fv.data(), dec.data(), imp.data());
+    handler->set_decision_level(1);
+    Decision last;
+    last.literal = mkLit(0, true);
+    last.decision_level = 1;
+    last.branched = false;
+    last.implicated_from_formula = false;
+    for (int64_t i = 0; i < trail_len; i++) {
+        int32_t d = trail[i];
+        Decision x;
+        x.literal = mkLit((d > 0 ? d : -d) - 1, d > 0);
+        x.decision_level = 1;
+        x.branched = false;
+        x.implicated_from_formula = false;
+        sat_status cur = handler->literal_status(x.literal);
+        if (cur == sat_status::UNSAT) return -2;
+        if (cur == sat_status::UNDEF) handler->new_decision(x);
+        last = x;
+    }
+    RuntimeStatistics stats(1, 1, nullptr);
+    auto *fs = new FullScan(n_vars, &formula, handler, false, 1, nullptr, &stats);
+    const Clause *confl = nullptr;
+    sat_status st = fs->sweep(last, &confl);
+    const int64_t k = (int64_t)handler->n_implications();
+    if (k > cap) return -1;
+    for (int64_t i = 0; i < k; i++) {
+        Lit l = handler->get_implication(i)->literal;
+        impl_lit[i] = sign(l) ? var(l) + 1 : -(var(l) + 1);
+    }
+    *n_impl = k;
+    if (st == sat_status::UNSAT) {
+        *conflict_clause = index.at(confl->literals);
+        return 1;
+    }
+    return 0;
 }
 
 /* Clauses after the reference's preprocessing and its initial watches. */

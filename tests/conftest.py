@@ -39,6 +39,15 @@ def bcp_golden():
 
 
 @pytest.fixture(scope="session")
+def scan_golden():
+    z = np.load(GOLDEN / "scan_golden.npz")
+    cases = []
+    for i in range(int(z["n_cases"][0])):
+        cases.append({k[len(f"c{i}_"):]: z[k] for k in z.files if k.startswith(f"c{i}_")})
+    return cases
+
+
+@pytest.fixture(scope="session")
 def preprocess_golden():
     z = np.load(GOLDEN / "preprocess_golden.npz")
     cases = []

@@ -5,6 +5,7 @@ Run in a container that has the reference sources, named by $GPSAT_REFERENCE
 
     GPSAT_REFERENCE=<reference checkout> python tests/golden/make_golden.py
     python tests/golden/make_golden.py --workload-only   # only the workload sample
+    python tests/golden/make_golden.py --scan-only       # only the full-scan vectors
 
 Outputs (committed):
   bcp_golden.npz     formulas + trails + the reference BCP's outputs
@@ -13,6 +14,9 @@ Outputs (committed):
                      through oracle/ref/ref_driver.cpp:ref_bcp
   preprocess_golden.npz  messy formulas and the reference's preprocessed
                      clauses, preprocessing verdict and initial watch positions
+  scan_golden.npz    formulas + trails + the outputs of the reference's
+                     full-scan clause evaluation (BASIC_SEARCH): status,
+                     conflict clause, implied literals in order
   solve_golden.json  the reference's six CNF fixtures (tests/cnf/*.cnf, with
                      their .expected verdicts) plus seeded random 3-SAT at
                      n=50 and the verdicts of the reference's sequential solver
@@ -219,6 +223,38 @@ def batch_cases():
     print("batch sample:", len(out), "decided by the reference:", sum(o["ref_nocap"] in (10, 20) for o in out))
 
 
+def scan_cases(ref):
+    """The reference's full-scan clause evaluation (ConflictAnalyzer::
+    propagate_all_clauses, driven through oracle/ref/ref_driver.cpp:ref_scan)
+    over seeded trails: status, conflict clause and the implied literals in
+    the order the sweeps found them."""
+    ref.ref_scan.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int64, vp, vp, vp]
+    specs = [(60, 256, 3, 31, 24, 0.05, 0.25), (200, 852, 3, 32, 24, 0.02, 0.15), (1000, 4200, 3, 33, 24, 0.01, 0.06),
+             (150, 1490, 5, 34, 24, 0.10, 0.50), (120, 700, 4, 35, 24, 0.05, 0.30)]
+    arrays = {}
+    for ci, (n, m, k, seed, T, lo, hi) in enumerate(specs):
+        lits, off = g.gen_random_ksat(seed, n, m, k)
+        tl, to = g.gen_trails(seed + 1000, n, T, lo, hi)
+        st = np.zeros(T, np.int32)
+        cc = np.zeros(T, np.int32)
+        ni = np.zeros(T, np.int64)
+        il = np.zeros((T, n), np.int32)
+        for t in range(T):
+            tr = np.ascontiguousarray(tl[to[t]:to[t + 1]])
+            a = np.zeros(n, np.int32)
+            k1 = np.zeros(1, np.int64)
+            c1 = np.zeros(1, np.int32)
+            st[t] = ref.ref_scan(P(lits), P(off), n, m, P(tr), len(tr), n, P(a), P(k1), P(c1))
+            cc[t], ni[t], il[t] = c1[0], k1[0], a
+        kmax = max(1, int(ni.max()))
+        for key, val in dict(n=np.array([n]), lits=lits, off=off, tl=tl, to=to, status=st, conflict=cc, n_impl=ni,
+                             impl_lit=il[:, :kmax]).items():
+            arrays[f"c{ci}_{key}"] = val
+        print(f"scan case {ci}: n={n} k={k} statuses={np.bincount(st + 2, minlength=4)[2:]} max_impl={ni.max()}")
+    arrays["n_cases"] = np.array([len(specs)])
+    np.savez_compressed(OUT / "scan_golden.npz", **arrays)
+
+
 def workload_cases(count=512, budget_s=30.0):
     """The reference's verdicts (iteration cap lifted) on the first `count`
     instances of the batched-solve workload (n ~ U[50, 250], ratio 4.26:
@@ -245,9 +281,13 @@ if __name__ == "__main__":
     if "--workload-only" in sys.argv:
         workload_cases()
         sys.exit(0)
+    if "--scan-only" in sys.argv:
+        scan_cases(load("stock"))
+        sys.exit(0)
     stock, nocap = load("stock"), load("nocap")
     bcp_cases(stock)
     preprocess_cases(stock)
     solve_cases(stock, nocap)
     batch_cases()
+    scan_cases(stock)
     workload_cases()

@@ -58,3 +58,18 @@ def test_oracle_rejects_conflicting_trail_and_accepts_repeats(orc):
     r2 = o.run(np.array([-3, -3], np.int32), np.array([0, 2], np.int64), impl_cap=8)
     assert r2["status"][0] in (0, 1)
     assert r2["counters"][0, 0] >= 2  # the repeated literal is propagated twice
+
+
+def test_oracle_full_scan_matches_reference_golden(orc, scan_golden):
+    """The full-scan restatement (the reference's BASIC_SEARCH) against the
+    reference's own propagate_all_clauses: status, conflict clause, implied
+    literals in order."""
+    for ci, c in enumerate(scan_golden):
+        n = int(c["n"][0])
+        r = orc.BCPOracle(c["lits"], c["off"], n).run(c["tl"], c["to"], impl_cap=n, strategy="full_scan")
+        for t in range(len(c["status"])):
+            k = int(c["n_impl"][t])
+            assert (r["status"][t], r["conflict"][t], r["n_impl"][t]) == (c["status"][t], c["conflict"][t], k), \
+                f"case {ci} trail {t}"
+            assert np.array_equal(r["impl_lit"][t, :k], c["impl_lit"][t, :k]), f"case {ci} trail {t}: implied literals"
+        assert (c["status"] == 1).any() and (c["status"] == 0).any()
