@@ -104,7 +104,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_gnn_mm": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32,
                                         ctypes.c_int32, _vp, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp]),
         "gpsat_gnn_wgrad": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
-                                           _vp, _vp]),
+                                           _vp, _vp, _vp]),
         "gpsat_gnn_gather": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int32, _vp, _vp,
                                             ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp]),
         "gpsat_gnn_gather_split": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int32, _vp, _vp, _vp,

@@ -21,8 +21,10 @@
 //                   accumulator back with tcgen05.ld and store bf16 rows.
 //                   Every linear map of the forward pass and every data
 //                   gradient of the backward pass is one call.
-//   wgrad_kernel    dW += X^T dY (weight gradients; K = rows is the long axis,
-//                   fp32 on the CUDA cores, one atomic add per output per block)
+//   wgrad_kernel    dW += X^T dY (weight gradients; K = rows is the long axis):
+//                   rows transposed into shared memory in register 8 x 8 blocks,
+//                   tcgen05.mma (M = 128 with X^T zero-padded, N, K = 16) into a
+//                   tensor-memory accumulator per block, double-buffered staging
 //   gather_kernel   out[s] = act( scale[s] * sum_e src_{sign e}[idx e] + Z[s] )
 //                   (message means: scale = 1 / degree)
 //   gather_split_kernel  outP[s], outN[s] = sums of scale[idx e] * src[idx e] over
@@ -232,69 +234,177 @@ __global__ void __launch_bounds__(128) mm_kernel(const __grid_constant__ CUtenso
 }
 
 // ---------------------------------------------------------------- weight gradients
-// dW[i][j] += sum_r X[r][i] * dY[r][j], i < 64, j < N <= 192.  256 threads;
-// each thread owns up to three 4 x 4 output blocks; rows stream through
-// shared memory in chunks of 32.
-constexpr int WG_ROWS = 32;
-constexpr int WG_MAXN = 192;
+// dW[64 x N] += X[rows x 64]^T dY[rows x N] on the tensor cores.  The long
+// axis (rows) is the contraction axis: a block takes chunks of WT_R rows
+// (strided over the grid) and, per chunk, its 128 threads transpose the rows
+// of X and dY in registers (8 x 8 bf16 blocks) into the no-swizzle K-major
+// operand layout above -- A = X^T as 128 rows (channels; rows 64..127 stay
+// zero), B = dY^T as N rows, K = the chunk's rows -- make the generic-proxy
+// writes visible to the tensor core (fence.proxy.async), and one thread
+// issues WT_R / 16 tcgen05.mma (M = 128, N, K = 16) accumulating into one fp32
+// matrix in tensor memory for all of the block's chunks.  Staging is double
+// buffered: the block fills one buffer while the tensor core reads the
+// other.  At the end warps 0-1 read lanes 0..63 back and add them into dW
+// (one atomic per output per block).
+constexpr int WT_R = 128;
+constexpr int WT_MAXN = 192;
 
-__global__ void __launch_bounds__(256) wgrad_kernel(const __nv_bfloat16 *X, int ldx, const __nv_bfloat16 *dY, int ldy,
-                                                    int rows, int N, float *dW)
+__device__ __forceinline__ void transpose8x8(const uint4 in[8], uint4 out[8])
 {
-    __shared__ float xs[WG_ROWS][64 + 4];
-    __shared__ float ys[WG_ROWS][WG_MAXN + 4];
-    const int nblk = 16 * (N / 4);  // 4x4 blocks
-    float acc[3][16];
+    // in[r] = row r (8 bf16: channels 0..7); out[c] = channel c (8 bf16: rows 0..7)
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(in);   // w[4 r + c / 2]
+    uint32_t *o = reinterpret_cast<uint32_t *>(out);
 #pragma unroll
-    for (int b = 0; b < 3; b++)
+    for (int c = 0; c < 8; c++)
 #pragma unroll
-        for (int q = 0; q < 16; q++) acc[b][q] = 0.f;
-    for (int r0 = blockIdx.x * WG_ROWS; r0 < rows; r0 += gridDim.x * WG_ROWS) {
-        __syncthreads();
-        for (int t = threadIdx.x; t < WG_ROWS * 32; t += 256) {
-            const int rr = t / 32, c = 2 * (t % 32);
-            float2 f = make_float2(0.f, 0.f);
-            if (r0 + rr < rows) f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(X + (size_t)(r0 + rr) * ldx + c));
-            xs[rr][c] = f.x;
-            xs[rr][c + 1] = f.y;
+        for (int q = 0; q < 4; q++)
+            o[4 * c + q] = __byte_perm(w[4 * (2 * q) + (c >> 1)], w[4 * (2 * q + 1) + (c >> 1)],
+                                       (c & 1) ? 0x7632 : 0x5410);
+}
+
+struct WgArgs {
+    const __nv_bfloat16 *X;
+    int ldx;
+    const __nv_bfloat16 *dY;
+    int ldy;
+    int rows, N;
+    float *dW;
+    int *err;
+};
+
+// Dynamic shared memory: [A 2 x 128*WT_R*2][B 2 x N*WT_R*2][2 mbarriers][tensor-memory address]
+__global__ void __launch_bounds__(128) wgrad_kernel(WgArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int N = a.N;
+    constexpr int ABYTES = 128 * WT_R * 2;
+    const int BBYTES = N * WT_R * 2;
+    unsigned char *As = sm;
+    unsigned char *Bs = sm + 2 * ABYTES;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(Bs + 2 * BBYTES);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t ncols = N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    const int nchunks = (a.rows + WT_R - 1) / WT_R;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the padding rows 64..127 of both A buffers are zero for good
+    for (int i = tid; i < 2 * ABYTES / 16; i += 128) {
+        const int buf = i / (ABYTES / 16), w = i % (ABYTES / 16);
+        const int row = (w % (128 * 16 / 16));   // 16-byte row inside its slab
+        if (row >= 64) reinterpret_cast<uint4 *>(As + buf * ABYTES)[w] = make_uint4(0, 0, 0, 0);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = instr_desc(128, N);
+
+    bool ok = true;
+    int issued = 0;                       // chunks multiplied by this block
+    uint32_t phase[2] = {0u, 0u};         // parity of each buffer's next completion
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int buf = issued & 1;
+        // the tensor core has finished reading this buffer (two chunks ago)
+        if (issued >= 2) {
+            bool w = true;
+            if (tid == 0) w = mbar_wait(&bars[buf], phase[buf]);
+            ok = __syncthreads_and(ok && w);
+            phase[buf] ^= 1u;
+            if (!ok) break;
         }
-        for (int t = threadIdx.x; t < WG_ROWS * (N / 2); t += 256) {
-            const int rr = t / (N / 2), c = 2 * (t % (N / 2));
-            float2 f = make_float2(0.f, 0.f);
-            if (r0 + rr < rows)
-                f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(dY + (size_t)(r0 + rr) * ldy + c));
-            ys[rr][c] = f.x;
-            ys[rr][c + 1] = f.y;
-        }
-        __syncthreads();
+        unsigned char *A = As + buf * ABYTES;
+        unsigned char *B = Bs + buf * BBYTES;
+        const int r0 = ch * WT_R;
+        // 8 x 8 blocks: X has (WT_R / 8) x 8 of them, dY (WT_R / 8) x (N / 8)
+        const int nbx = (WT_R / 8) * 8, nby = (WT_R / 8) * (N / 8);
+        for (int bkt = tid; bkt < nbx + nby; bkt += 128) {
+            const bool isx = bkt < nbx;
+            const int b = isx ? bkt : bkt - nbx;
+            const int cols = isx ? 8 : N / 8;
+            const int rb = b / cols, cb = b % cols;
+            const __nv_bfloat16 *src = isx ? a.X : a.dY;
+            const int ld = isx ? a.ldx : a.ldy;
+            uint4 in[8], out[8];
 #pragma unroll
-        for (int b = 0; b < 3; b++) {
-            const int blk = threadIdx.x + 256 * b;
-            if (blk < nblk) {
-                const int bi = (blk % 16) * 4, bj = (blk / 16) * 4;
-                for (int rr = 0; rr < WG_ROWS; rr++) {
-                    const float4 xv = *reinterpret_cast<const float4 *>(&xs[rr][bi]);
-                    const float4 yv = *reinterpret_cast<const float4 *>(&ys[rr][bj]);
-                    const float xa[4] = {xv.x, xv.y, xv.z, xv.w}, ya[4] = {yv.x, yv.y, yv.z, yv.w};
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int j = 0; j < 4; j++) acc[b][4 * i + j] += xa[i] * ya[j];
-                }
+            for (int r = 0; r < 8; r++) {
+                const int row = r0 + 8 * rb + r;
+                in[r] = row < a.rows ? *reinterpret_cast<const uint4 *>(src + (size_t)row * ld + 8 * cb)
+                                     : make_uint4(0, 0, 0, 0);
             }
+            transpose8x8(in, out);
+            // operand row (channel) 8 cb + c, K elements [8 rb, 8 rb + 8): slab rb
+            unsigned char *dst = isx ? A + rb * (128 * 16) : B + rb * (N * 16);
+#pragma unroll
+            for (int c = 0; c < 8; c++) *reinterpret_cast<uint4 *>(dst + (8 * cb + c) * 16) = out[c];
         }
-    }
-#pragma unroll
-    for (int b = 0; b < 3; b++) {
-        const int blk = threadIdx.x + 256 * b;
-        if (blk < nblk) {
-            const int bi = (blk % 16) * 4, bj = (blk / 16) * 4;
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) atomicAdd(&dW[(size_t)(bi + i) * N + bj + j], acc[b][4 * i + j]);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) {
+            const uint32_t aa = smem_u32(A), ba = smem_u32(B);
+            for (int k = 0; k < WT_R / 16; k++) {
+                const uint64_t ad = smem_desc(aa + 2 * k * 128 * 16, 128 * 16, 128);
+                const uint64_t bd = smem_desc(ba + 2 * k * N * 16, N * 16, 128);
+                const uint32_t acc = (issued > 0 || k > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&bars[buf]))
+                         : "memory");
         }
+        issued++;
     }
+    // wait for the products still in flight (the last one or two buffers)
+    for (int k = issued >= 2 ? issued - 2 : 0; k < issued && ok; k++) {
+        const int buf = k & 1;
+        bool w = true;
+        if (tid == 0) w = mbar_wait(&bars[buf], phase[buf]);
+        ok = __syncthreads_and(ok && w);
+        phase[buf] ^= 1u;
+    }
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && issued > 0 && warp < 2) {
+        // warp w reads tensor-memory lanes [32w, 32w + 32): dW row 32w + lane
+        const int i = warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                "[%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(lane_base + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 32; q++) atomicAdd(&a.dW[(size_t)i * N + c0 + q], __uint_as_float(v[q]));
+        }
+    } else if (!ok && tid == 0 && a.err) {
+        atomicExch(a.err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
 // ---------------------------------------------------------------- message sums
@@ -572,17 +682,30 @@ extern "C" int gpsat_gnn_mm(const void *X, int32_t ldx, int64_t rows, int32_t K,
 }
 
 extern "C" int gpsat_gnn_wgrad(const void *X, int32_t ldx, const void *dY, int32_t ldy, int64_t rows, int32_t N,
-                               float *dW, void *stream)
+                               float *dW, int32_t *err, void *stream)
 {
-    if (rows < 0 || rows > INT32_MAX || N <= 0 || N > gnn::MAXN || N % 4 || ldx < 64 || ldy < N ||
-        (rows > 0 && (!X || !dY || !dW)))
-        return set_error(GPSAT_ERR_ARG, "gpsat_gnn_wgrad: bad argument");
+    if (rows < 0 || rows > INT32_MAX || N <= 0 || N > gnn::WT_MAXN || N % 64 || ldx < 64 || ldy < N || ldx % 8 ||
+        ldy % 8 || (rows > 0 && (!X || !dY || !dW)))
+        return set_error(GPSAT_ERR_ARG, "gpsat_gnn_wgrad: need N in {64, 128, 192}, row strides multiples of 8");
     if (rows == 0) return GPSAT_OK;
-    if (N > gnn::WG_MAXN) return set_error(GPSAT_ERR_ARG, "gpsat_gnn_wgrad: N <= 192");
-    const int grid = (int)std::min<int64_t>((rows + gnn::WG_ROWS - 1) / gnn::WG_ROWS, 152 * 4);
-    gnn::wgrad_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(static_cast<const __nv_bfloat16 *>(X), ldx,
-                                                             static_cast<const __nv_bfloat16 *>(dY), ldy, (int)rows,
-                                                             N, dW);
+    if (((uintptr_t)X & 15) || ((uintptr_t)dY & 15))
+        return set_error(GPSAT_ERR_ARG, "gpsat_gnn_wgrad: X and dY must be 16-byte aligned");
+    const size_t smem = 2 * (size_t)128 * gnn::WT_R * 2 + 2 * (size_t)N * gnn::WT_R * 2 + 2 * 8 + 16;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(gnn::wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(2 * 128 * gnn::WT_R * 2 + 2 * gnn::WT_MAXN * gnn::WT_R * 2 + 64));
+    });
+    if (attr != cudaSuccess) return cuda_error(attr, "gpsat_gnn_wgrad: shared memory attribute");
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t chunks = (rows + gnn::WT_R - 1) / gnn::WT_R;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(chunks, sms));
+    gnn::WgArgs a{static_cast<const __nv_bfloat16 *>(X), ldx, static_cast<const __nv_bfloat16 *>(dY), ldy,
+                  (int)rows, N, dW, err};
+    gnn::wgrad_kernel<<<grid, 128, smem, (cudaStream_t)stream>>>(a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GPSAT_OK : cuda_error(e, "gpsat_gnn_wgrad launch");
 }

@@ -250,16 +250,18 @@ class Pass:
             # H_c^{l+1} feeds B (this layer) and Zc of the layer above
             K = 3 * D if l + 1 < LAYERS else 2 * D
             self.mm(_p(gc), 3 * D, C, K, net.bwd_c[l], D, None, _p(dHc), D, stream)
-            check(L.gpsat_gnn_wgrad(_p(self.Hc[l + 1]), D, _p(gc), 3 * D, C, 2 * D, net.ptr(f"U_{l}", True), stream))
+            check(L.gpsat_gnn_wgrad(_p(self.Hc[l + 1]), D, _p(gc), 3 * D, C, 2 * D, net.ptr(f"U_{l}", True),
+                                    _p(self.err), stream))
             # through H_c^{l+1} = relu(sum A + Zc); dPreC goes to the other buffer's last third
             check(L.gpsat_gnn_relu_bwd(_p(dHc), D, _p(self.Hc[l + 1]), D, C, _off(gc_next, 2 * D), 3 * D, stream))
             check(L.gpsat_gnn_wgrad(_p(self.Hc[l]), D, _off(gc_next, 2 * D), 3 * D, C, D, net.ptr(f"Wc_{l}", True),
-                                    stream))
+                                    _p(self.err), stream))
             check(L.gpsat_gnn_colsum(_off(gc_next, 2 * D), 3 * D, C, net.ptr(f"bc_{l}", True), stream))
             check(L.gpsat_gnn_gather_split(_p(g.v_off), _p(g.v_edges), V, _off(gc_next, 2 * D), 3 * D,
                                            _p(g.c_scale), _p(GV), _off(GV, D), 3 * D, stream))
             # A3 = H_v^l Wv3 + bias3
-            check(L.gpsat_gnn_wgrad(_p(self.Hv[l]), D, _p(GV), 3 * D, V, 3 * D, net.ptr(f"Wv3_{l}", True), stream))
+            check(L.gpsat_gnn_wgrad(_p(self.Hv[l]), D, _p(GV), 3 * D, V, 3 * D, net.ptr(f"Wv3_{l}", True),
+                                    _p(self.err), stream))
             check(L.gpsat_gnn_colsum(_off(GV, 2 * D), 3 * D, V, net.ptr(f"bias3_{l}", True) + 4 * 2 * D, stream))
             self.mm(_p(GV), 3 * D, V, 3 * D, net.bwd_v[l], D, None, _p(dHv), D, stream)
             if l == 0:
@@ -268,7 +270,7 @@ class Pass:
                 check(L.gpsat_gnn_colsum(_p(dHc), D, C, net.ptr("hc0", True), stream))
                 # H_v^0 = relu(F Win + bin)
                 check(L.gpsat_gnn_relu_bwd(_p(dHv), D, _p(self.Hv[0]), D, V, _p(dHv), D, stream))
-                check(L.gpsat_gnn_wgrad(_p(g.feat), D, _p(dHv), D, V, D, net.ptr("Win", True), stream))
+                check(L.gpsat_gnn_wgrad(_p(g.feat), D, _p(dHv), D, V, D, net.ptr("Win", True), _p(self.err), stream))
                 check(L.gpsat_gnn_colsum(_p(dHv), D, V, net.ptr("bin", True), stream))
 
 

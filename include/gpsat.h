@@ -333,9 +333,11 @@ int gpsat_gen_planted(uint64_t seed, int32_t n_vars, int64_t n_clauses, int32_t 
 int gpsat_gnn_mm(const void *X, int32_t ldx, int64_t rows, int32_t K, const void *B, int32_t ldb,
                  int32_t N, const float *bias, int32_t relu, void *Y, int32_t ldy, int32_t *err,
                  void *stream);
-/* dW[64 x N] += X[rows x 64]^T . dY[rows x N] (fp32 dW, N <= 192, N % 4 == 0) */
+/* dW[64 x N] += X[rows x 64]^T . dY[rows x N] (fp32 dW, N in {64, 128, 192});
+ * tcgen05 tensor cores, the rows being the contraction axis.  *err (may be
+ * NULL) is set to 1 if a block gave up waiting for its products. */
 int gpsat_gnn_wgrad(const void *X, int32_t ldx, const void *dY, int32_t ldy, int64_t rows, int32_t N,
-                    float *dW, void *stream);
+                    float *dW, int32_t *err, void *stream);
 /* out[s] = act(seg_scale[s] * sum over edges e of s of (positive ? srcP : srcN)[row e] + Z[s]),
  * 64 channels; act = relu when relu != 0; seg_scale and Z may be NULL */
 int gpsat_gnn_gather(const int64_t *seg_off, const int32_t *edges, int64_t segs, const void *srcP,

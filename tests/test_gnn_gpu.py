@@ -44,17 +44,25 @@ def test_mm_matches_torch(gpsat, torch_dev, rows, K, N, ld_extra):
     close(Y, want, rtol=1e-2, atol=2e-2)
 
 
-def test_wgrad_matches_torch(gpsat, torch_dev):
+@pytest.mark.parametrize("rows,N,ldx_extra,ldy_extra", [(3001, 192, 0, 0), (128, 64, 8, 64), (40000, 128, 128, 64),
+                                                      (77, 64, 0, 0)])
+def test_wgrad_matches_torch(gpsat, torch_dev, rows, N, ldx_extra, ldy_extra):
+    """dW += X^T dY on the tensor cores (rows are the contraction axis, in
+    chunks of 128 with a ragged last one), row strides wider than the data."""
     torch, dev = torch_dev
     g = torch.Generator(device="cpu").manual_seed(7)
-    rows, N = 3001, 192
-    X = torch.randn(rows, 64, generator=g).to(dev, torch.bfloat16)
-    dY = torch.randn(rows, N, generator=g).to(dev, torch.bfloat16)
-    dW = torch.zeros(64, N, device=dev)
-    gpsat.check(gpsat.lib().gpsat_gnn_wgrad(X.data_ptr(), 64, dY.data_ptr(), N, rows, N, dW.data_ptr(), None))
+    Xw = torch.randn(rows, 64 + ldx_extra, generator=g).to(dev, torch.bfloat16)
+    Yw = torch.randn(rows, N + ldy_extra, generator=g).to(dev, torch.bfloat16)
+    X, dY = Xw[:, :64], Yw[:, :N]
+    dW = torch.full((64, N), 0.5, device=dev)          # accumulates into what is there
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    gpsat.check(gpsat.lib().gpsat_gnn_wgrad(X.data_ptr(), 64 + ldx_extra, dY.data_ptr(), N + ldy_extra, rows, N,
+                                            dW.data_ptr(), err.data_ptr(), None))
     torch.cuda.synchronize()
-    want = X.float().T @ dY.float()
-    close(dW, want, rtol=1e-4, atol=1e-3)           # fp32 accumulation of exact bf16 products
+    assert err.item() == 0
+    want = X.float().T @ dY.float() + 0.5
+    # fp32 accumulation of exact bf16 products, summed in another order
+    close(dW, want, rtol=1e-4, atol=2e-3 * (rows / 3000) ** 0.5 + 1e-3)
 
 
 def test_gather_and_split_match_torch(gpsat, torch_dev):
@@ -189,18 +197,23 @@ def test_training_lowers_the_loss(gpsat, torch_dev):
 
 
 def test_learned_seeding_against_plain_vsids(gpsat, torch_dev):
-    """What the trained network gains over the plain solver on held-out random
-    3-SAT (n in [150, 250], ratio 4.26): verdicts agree wherever both decide,
-    every model checks, and the seeded arm's median conflict count is reported
-    against the plain arm's (it must not be worse by more than noise)."""
+    """What the trained network gains over the plain solver: trained (every
+    forward and backward step in the library's kernels) on labels the plain
+    solver logs on 2,048 random k-SAT training formulas (k in {3, 4, 5} near
+    threshold, n in [100, 400]), then 1,024 held-out instances of the batched
+    workload's distribution (random 3-SAT, n in [50, 250], ratio 4.26; formula
+    seeds the workload does not use) are solved plain and seeded.  Verdicts
+    agree wherever both decide, every model checks, and the seeded arm needs
+    fewer conflicts at the median."""
     torch, dev = torch_dev
     from gpupsat_gb300 import learn
+    torch.manual_seed(0)
     net = learn.SeedNet(dev, seed=0)
-    learn.train(net, learn.training_set(512, seed=3), epochs=3, conflict_budget=10000, log=None)
-    rng = np.random.default_rng(23)
-    ns = [int(n) for n in rng.integers(150, 251, size=384)]
+    learn.train(net, learn.training_set(2048, seed=0), epochs=3, conflict_budget=20000, log=None)
+    rng = np.random.default_rng(29)
+    ns = [int(n) for n in rng.integers(50, 251, size=1024)]
     formulas = [gpsat.gen_random_ksat(90000 + i, n, int(round(4.26 * n)), 3) for i, n in enumerate(ns)]
-    opts = gpsat.solve_options(conflict_budget=20000)
+    opts = gpsat.solve_options(conflict_budget=100000)
     plain = gpsat.Batch(formulas, ns).solve(opts)
     score, phase = learn.predict(net, formulas, ns)
     b = gpsat.Batch(formulas, ns)
@@ -210,7 +223,9 @@ def test_learned_seeding_against_plain_vsids(gpsat, torch_dev):
     both = (vp != 0) & (vs != 0)
     assert (vp[both] == vs[both]).all()
     assert (seeded["model_ok"][vs == gpsat.SAT] == 1).all()
-    mp, ms = np.median(plain["stats"][:, 0]), np.median(seeded["stats"][:, 0])
+    cp, cs = plain["stats"][:, 0], seeded["stats"][:, 0]
+    mp, ms = np.median(cp), np.median(cs)
     print(f"median conflicts: plain {mp:.0f}, seeded {ms:.0f} ({100 * (1 - ms / mp):+.1f}% fewer); "
-          f"decided: plain {int((vp != 0).sum())}, seeded {int((vs != 0).sum())}")
-    assert ms <= 1.05 * mp
+          f"mean {cp.mean():.0f} vs {cs.mean():.0f}; decided: plain {int((vp != 0).sum())}, "
+          f"seeded {int((vs != 0).sum())}; seeded fewer on {(cs < cp).mean():.2%} of instances")
+    assert ms < mp
