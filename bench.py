@@ -565,7 +565,9 @@ def solve_object_gpu(args, count, steps=1):
     h2d = sum(l.nbytes + o.nbytes for l, o in formulas)
     d2h = int(out["verdict"].nbytes + out["model"].nbytes + out["stats"].nbytes + out["model_ok"].nbytes)
     b.close()
+    cert = certify_sample(args, formulas[:256], nv[:256], out["verdict"][:256])
     return {"metric": SOLVE_METRIC, "value": decided * steps / sum(times), "unit": "instances/s",
+            "unsat_certified": cert,
             "steps": steps, "warmup": 1, "ms_per_step": 1000 * sum(times) / steps,
             "config": solve_config(args, count),
             "e2e": {"value": decided / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": int(h2d),
@@ -578,6 +580,33 @@ def solve_object_gpu(args, count, steps=1):
             "conflicts_per_s": float(st[:, 0].sum()) * steps / sum(times),
             "props_per_s": float(st[:, 2].sum()) * steps / sum(times), "clocks": clk,
             "gpu_launches": 2 * steps}
+
+
+def certify_sample(args, formulas, nv, verdicts):
+    """UNSAT verdicts certified independently of the reference: the first
+    instances solved again with the device proof log on, every UNSAT job's
+    learnt clauses checked on the host by reverse unit propagation
+    (gpsat_check_rup) against the original clauses; where both runs decide,
+    the verdicts must equal the timed run's."""
+    import gpupsat_gb300 as g
+    b = g.Batch(formulas, nv)
+    opts = g.solve_options(conflict_budget=args.conflict_budget)
+    out = b.solve(opts, proof_words=1 << 22)
+    v = out["verdict"]
+    both = (v != 0) & (verdicts != 0)
+    if not np.array_equal(v[both], verdicts[both]):
+        raise AssertionError("certification sample: verdicts differ from the timed run")
+    t0 = time.perf_counter()
+    cert = b.certify_unsat(v)
+    dt = time.perf_counter() - t0
+    ok = sum(1 for r in cert.values() if r[0])
+    if ok != int((v == 20).sum()):
+        raise AssertionError(f"certification sample: {int((v == 20).sum()) - ok} UNSAT proofs rejected")
+    b.close()
+    return {"instances": len(nv), "unsat": int((v == 20).sum()), "rup_certified": ok,
+            "same_verdict_as_timed_run": int((v == verdicts).sum()),
+            "check_seconds": round(dt, 2),
+            "checker": "gpsat_check_rup (host, reverse unit propagation over the device proof log)"}
 
 
 def solve_object_ref(args):
