@@ -330,15 +330,15 @@ def run_gpu(args):
     for _ in range(args.warmup):
         b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
     stream.synchronize()
-    # trails in flight: a launch lasts as long as its longest trails, which
-    # wait on memory the other trails load too, so fewer slots can finish
-    # sooner; chosen on untimed launches (outputs do not depend on it)
+    # the autotuner: window width (watch entries per round: threads per
+    # trail) and trails in flight, chosen on untimed launches (outputs do not
+    # depend on them)
     if args.slots is None:
-        tuning = b.tune_slots(d_tl, d_to, out, stream.cuda_stream)
+        tuning = b.tune(d_tl, d_to, out, stream.cuda_stream)
     else:
         b.set_active_slots(args.slots)
         tuning = None
-    active = b.active or b.info()["slots"]
+    active = b.active or b.window_slots(b.window)
     cnt = out["counters"].cpu().numpy()
     props_step = int(cnt[:, 0].sum())
     bytes_step = alg_bytes(cnt)
@@ -394,7 +394,7 @@ def run_gpu(args):
     achieved = bytes_step / avg_launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic_per_launch(n, T), "peak_source": peak_src,
-            "alg_bytes_per_launch": bytes_step, "kernel": "gpsat::bcp::bcp_kernel"}
+            "alg_bytes_per_launch": bytes_step, "kernel": "bcp_kernel"}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -408,10 +408,11 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
             "config": config(args, n, m),
-            "launch": {"slots": active,
-                       "slot_tuning_ms": {str(k): round(v, 3) for k, v in tuning.items()} if tuning else None},
+            "launch": {"window": b.window, "threads_per_trail": b.window, "slots": active,
+                       "tuning_ms": {f"{w}x{n}": round(v, 3) for (w, n), v in tuning.items()} if tuning else None},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": args.steps * (4 if T > active else 1),  # order kernels + BCP kernel
+            "kernel": f"gpsat::bcp::w{b.window // 32}::bcp_kernel",
             "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item()),
             "check": check}
     del out, d_tl, d_to

@@ -78,6 +78,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_bcp_info": (ctypes.c_int, [_vp, _c_i32p, _c_i64p]),
         "gpsat_bcp_set_active_slots": (ctypes.c_int, [_vp, ctypes.c_int32]),
         "gpsat_bcp_set_strategy": (ctypes.c_int, [_vp, ctypes.c_int32]),
+        "gpsat_bcp_set_window": (ctypes.c_int, [_vp, ctypes.c_int32]),
+        "gpsat_bcp_window_slots": (ctypes.c_int, [_vp, ctypes.c_int32, _c_i32p]),
         "gpsat_bcp_run_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 8),
         "gpsat_bcp_run_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 7),
         "gpsat_bcp_run_static": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp, ctypes.c_int32]
@@ -259,11 +261,56 @@ class BCPBatch:
         self._h = _vp()
         check(lib().gpsat_bcp_create(formula.handle, max_slots, impl_cap, arena_cap, ctypes.byref(self._h)))
         self.active = 0
+        self.window = 128
+        self.strategy = "watched"
 
     def info(self) -> dict:
         s, b = ctypes.c_int32(), ctypes.c_int64()
         check(lib().gpsat_bcp_info(self._h, ctypes.byref(s), ctypes.byref(b)))
         return dict(slots=s.value, device_bytes=b.value)
+
+    def window_slots(self, entries: int) -> int:
+        """Trails the window width keeps in flight at most."""
+        n = ctypes.c_int32()
+        check(lib().gpsat_bcp_window_slots(self._h, int(entries), ctypes.byref(n)))
+        return n.value
+
+    def set_window(self, entries: int) -> None:
+        """Watch entries per round of the two-watched-literal kernel (64, 128
+        or 256); outputs do not depend on it."""
+        check(lib().gpsat_bcp_set_window(self._h, int(entries)))
+        self.window = int(entries)
+
+    def tune(self, trail_lits, trail_offsets, out: dict, stream: int, windows=(128, 256, 64),
+             fractions=(1.0, 0.75, 0.5)):
+        """The BCP autotuner: times one run_device launch of these trails (after
+        one untimed launch) for every window width and, at each width, every
+        fraction of the slots that width keeps resident; keeps the fastest
+        pair.  Returns {(window, active slots): ms}.  Outputs do not depend on
+        the setting; `out` holds the last launch's results."""
+        import torch
+        st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        slots = self.info()["slots"]
+        times = {}
+        for w in windows:
+            self.set_window(w)
+            per = self.window_slots(w)
+            for f in fractions:
+                n = max(4, int(per * f) // 4 * 4)
+                if n > slots:
+                    continue
+                self.set_active_slots(n)
+                self.run_device(trail_lits, trail_offsets, out, stream=stream)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                self.run_device(trail_lits, trail_offsets, out, stream=stream)
+                b.record(st)
+                b.synchronize()
+                times[(w, n)] = a.elapsed_time(b)
+        (w, n) = min(times, key=times.get)
+        self.set_window(w)
+        self.set_active_slots(n)
+        return times
 
     def set_strategy(self, strategy: str) -> None:
         """"watched" (two watched literals, the default) or "full_scan" (the
@@ -276,29 +323,6 @@ class BCPBatch:
         """Later runs use at most n slots (0 = all); outputs do not depend on it."""
         check(lib().gpsat_bcp_set_active_slots(self._h, int(n)))
         self.active = int(n)
-
-    def tune_slots(self, trail_lits, trail_offsets, out: dict, stream: int, fractions=(1.0, 0.75, 0.5, 0.375)):
-        """Times one run_device launch of these trails at each fraction of the
-        slots (after one untimed launch) on `stream`, keeps the fastest setting
-        and returns {active slots: ms}.  The trails and `out` are as for
-        run_device; the results in `out` are those of the last launch."""
-        import torch
-        slots = self.info()["slots"]
-        cands = sorted({max(4, int(slots * f) // 4 * 4) for f in fractions if f > 0} & set(range(1, slots + 1)),
-                       reverse=True)
-        st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
-        times = {}
-        for n in cands:
-            self.set_active_slots(n)
-            self.run_device(trail_lits, trail_offsets, out, stream=stream)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(st)
-            self.run_device(trail_lits, trail_offsets, out, stream=stream)
-            b.record(st)
-            b.synchronize()
-            times[n] = a.elapsed_time(b)
-        self.set_active_slots(min(times, key=times.get))
-        return times
 
     def host_outputs(self, n_trails: int, counters: bool = True, alloc=np.zeros) -> dict:
         """Output arrays for run_host (alloc may return pinned memory, e.g. numpy

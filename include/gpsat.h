@@ -157,6 +157,15 @@ int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n);
  * Trails run one per thread block; a formula of up to 196,608 variables keeps a
  * trail's assignment in shared memory.  gpsat_bcp_run_static always runs
  * GPSAT_BCP_WATCHED. */
+/* Watch entries one round of the two-watched-literal kernel evaluates per
+ * trail (64, 128 or 256; default 128): one thread per entry, so the trail's
+ * thread block has entries / 32 warps.  Wider windows need fewer rounds per
+ * propagation but keep fewer trails in flight; outputs do not depend on it.
+ * (No counterpart in the reference, whose BCP is one thread per solver.) */
+int gpsat_bcp_set_window(gpsat_bcp *b, int32_t entries);
+/* Trails a window width keeps in flight at most: its resident blocks, within
+ * the workspace's slots. */
+int gpsat_bcp_window_slots(const gpsat_bcp *b, int32_t entries, int32_t *slots);
 #define GPSAT_BCP_WATCHED 0
 #define GPSAT_BCP_FULL_SCAN 1
 int gpsat_bcp_set_strategy(gpsat_bcp *b, int32_t strategy);

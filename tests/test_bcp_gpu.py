@@ -208,3 +208,37 @@ def test_bcp_full_size_benchmark_shape(gpsat, orc, cuda_ok):
         if g["status"][t] == 1:
             c = cl[g["conflict"][t]]
             assert (sgn[np.abs(c)] == -np.sign(c)).all(), f"trail {t}: conflict clause not false"
+
+
+def test_bcp_window_widths_agree(gpsat, orc, cuda_ok):
+    """The kernel at 64, 128 and 256 watch entries per round (2, 4 and 8 warps
+    per trail): the same outputs and counters, equal to the oracle's; the
+    autotuner picks one of them."""
+    import torch
+    n = 20000
+    lits, off = gpsat.gen_random_ksat(44, n, 84000, 3)
+    tl, to = gpsat.gen_trails(45, n, 300, 0.01, 0.05)
+    b = gpsat.BCPBatch(gpsat.Formula(lits, off, n), impl_cap=2048)
+    o = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=2048, threads=8)
+    for w in (64, 256, 128):
+        b.set_window(w)
+        assert b.window_slots(w) >= 1
+        g = b.run_host(tl, to)
+        compare_bcp(g, o, label=f"window {w}")
+        assert np.array_equal(g["counters"], o["counters"])
+    with pytest.raises(gpsat.GpsatError):
+        b.set_window(96)
+    dev = torch.device("cuda:0")
+    T = len(to) - 1
+    out = dict(status=torch.empty(T, dtype=torch.int32, device=dev),
+               conflict=torch.empty(T, dtype=torch.int32, device=dev),
+               stop=torch.empty(T, dtype=torch.int32, device=dev),
+               n_impl=torch.empty(T, dtype=torch.int64, device=dev),
+               impl_lit=torch.empty(T, 2048, dtype=torch.int32, device=dev),
+               impl_reason=torch.empty(T, 2048, dtype=torch.int32, device=dev),
+               counters=torch.empty(T, 6, dtype=torch.int64, device=dev))
+    s = torch.cuda.Stream()
+    times = b.tune(torch.from_numpy(tl).to(dev), torch.from_numpy(to).to(dev), out, s.cuda_stream)
+    assert b.window in (64, 128, 256) and (b.window, b.active) in times
+    s.synchronize()
+    compare_bcp({k: v.cpu().numpy() for k, v in out.items()}, o, label="after tuning")
