@@ -74,8 +74,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-trails", type=int, default=4096)
     ap.add_argument("--slots", type=int, default=None,
-                    help="bcp: trails in flight (default: the fastest of 1, 3/4, 1/2, 3/8 of the resident "
-                         "warps, timed on warm-up launches)")
+                    help="bcp: trails in flight (default: the autotuner's choice, timed on warm-up launches)")
+    ap.add_argument("--arena-cap", type=int, default=0,
+                    help="bcp: added watch entries per trail slot (default: the library's, 2^17)")
+    ap.add_argument("--window", type=int, default=None, choices=[64, 128, 256],
+                    help="bcp: watch entries per round and trail (default: the autotuner's choice); with "
+                         "--slots, no tuning launch runs")
     ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding"],
                     help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
                          "planted: planted community instances split into JobChooser cubes; "
@@ -119,7 +123,7 @@ def config(args, n, m):
     return {"workload": "BCP microbenchmark: random 3-SAT, partial trails",
             "n_vars": n, "n_clauses": m, "n_trails": args.trails, "trail_fraction": [0.01, 0.05],
             "literal_arena": "int32 CSR", "l2": "inputs larger than L2 (formula 0.3 GB, trails 0.5 GB, "
-                                               "per-trail state > 30 GB); no flush needed",
+                                               "per-trail state 25 MB per slot, > 15 GB in flight); no flush needed",
             "semantics": "reference order (bit-exact reasons and conflict clause)"}
 
 
@@ -316,7 +320,8 @@ def run_gpu(args):
     T = args.trails
     cap = args.impl_cap
     f = g.Formula(lits, off, n)
-    b = g.BCPBatch(f, impl_cap=cap)
+    # with --slots fixed, only those slots are allocated (no tuning launches)
+    b = g.BCPBatch(f, impl_cap=cap, max_slots=args.slots or 0, arena_cap=args.arena_cap)
     d_tl = torch.from_numpy(tl).to(dev)
     d_to = torch.from_numpy(to).to(dev)
     out = dict(status=torch.empty(T, dtype=torch.int32, device=dev),
@@ -327,6 +332,8 @@ def run_gpu(args):
                impl_reason=torch.empty(T, cap, dtype=torch.int32, device=dev),
                counters=torch.empty(T, 6, dtype=torch.int64, device=dev))
     stream = torch.cuda.Stream(device=dev)
+    if args.window is not None:
+        b.set_window(args.window)
     for _ in range(args.warmup):
         b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
     stream.synchronize()
@@ -334,7 +341,8 @@ def run_gpu(args):
     # trail) and trails in flight, chosen on untimed launches (outputs do not
     # depend on them)
     if args.slots is None:
-        tuning = b.tune(d_tl, d_to, out, stream.cuda_stream)
+        windows = (args.window,) if args.window is not None else (128, 256, 64)
+        tuning = b.tune(d_tl, d_to, out, stream.cuda_stream, windows=windows)
     else:
         b.set_active_slots(args.slots)
         tuning = None
@@ -394,7 +402,7 @@ def run_gpu(args):
     achieved = bytes_step / avg_launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic_per_launch(n, T), "peak_source": peak_src,
-            "alg_bytes_per_launch": bytes_step, "kernel": "bcp_kernel"}
+            "alg_bytes_per_launch": bytes_step, "kernel": f"gpsat::bcp::w{b.window // 32}::bcp_kernel"}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1

@@ -253,7 +253,7 @@ class Formula:
 
 # ---------------------------------------------------------------- BCP batch
 class BCPBatch:
-    """Reference-order two-watched-literal BCP over many partial trails (one warp per trail)."""
+    """Reference-order two-watched-literal BCP over many partial trails (one thread block per trail)."""
 
     def __init__(self, formula: Formula, max_slots: int = 0, impl_cap: int = 4096, arena_cap: int = 0):
         self.formula = formula
