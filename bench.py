@@ -80,8 +80,9 @@ def parse():
     ap.add_argument("--window", type=int, default=None, choices=[64, 128, 256],
                     help="bcp: watch entries per round and trail (default: the autotuner's choice); with "
                          "--slots, no tuning launch runs")
-    ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding"],
-                    help="bcp: the BCP microbenchmark (default); solve: batched random 3-SAT solving; "
+    ap.add_argument("--workload", default="bcp", choices=["bcp", "solve", "planted", "seeding", "full_scan"],
+                    help="bcp: the BCP microbenchmark (default); full_scan: the same trails under the "
+                         "reference's full-scan clause evaluation; solve: batched random 3-SAT solving; "
                          "planted: planted community instances split into JobChooser cubes; "
                          "seeding: learned VSIDS/phase seeding against plain solving")
     ap.add_argument("--n-range", type=int, nargs=2, default=[50, 250], help="solve: variables per instance")
@@ -120,10 +121,16 @@ def workload(args, rank, gen=None):
 
 
 def config(args, n, m):
+    formula = m * 3 * 4 + m * 4 + n * 4 + 2 * m * 32          # literals, offsets, list offsets, initial watches
+    trails = args.trails * 0.03 * n * 4                         # 1-5% of n per trail, int32
+    slot = n // 16 * 4 + n * 4 + m * 4 + (args.arena_cap or (1 << 17)) * 32
+    big = formula + trails > 256e6
     return {"workload": "BCP microbenchmark: random 3-SAT, partial trails",
             "n_vars": n, "n_clauses": m, "n_trails": args.trails, "trail_fraction": [0.01, 0.05],
-            "literal_arena": "int32 CSR", "l2": "inputs larger than L2 (formula 0.3 GB, trails 0.5 GB, "
-                                               "per-trail state 25 MB per slot, > 15 GB in flight); no flush needed",
+            "literal_arena": "int32 CSR",
+            "l2": f"formula {formula / 1e9:.3g} GB, trails {trails / 1e9:.3g} GB, per-trail state "
+                  f"{slot / 1e6:.3g} MB per slot" + ("; inputs larger than L2, no flush needed" if big else
+                                                    "; the formula fits L2 (a small case)"),
             "semantics": "reference order (bit-exact reasons and conflict clause)"}
 
 
@@ -196,17 +203,18 @@ def alg_bytes(cnt):
     return 4 * W + 4 * L + A + 9 * I + 5 * T
 
 
-def cpu_baseline(lits, off, n, tl, to, ntrails, threads):
-    """The oracle on the first `ntrails` trails with `threads` host threads."""
+def cpu_baseline(lits, off, n, tl, to, ntrails, threads, strategy="watched"):
+    """The oracle on the first `ntrails` trails with `threads` host threads.
+    Units: propagations (watched) or clause evaluations (full_scan)."""
     import oracle
     o = oracle.BCPOracle(lits, off, n)
     T = min(ntrails, len(to) - 1)
     sub_to = to[:T + 1].copy()
     sub_tl = tl[:sub_to[-1]]
     t0 = time.perf_counter()
-    r = o.run(sub_tl, sub_to, impl_cap=4096, threads=threads)
+    r = o.run(sub_tl, sub_to, impl_cap=4096, threads=threads, strategy=strategy)
     dt = time.perf_counter() - t0
-    props = int(r["counters"][:, 0].sum())
+    props = int(r["counters"][:, 1 if strategy == "full_scan" else 0].sum())
     return props / dt, props, dt, T
 
 
@@ -436,7 +444,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def bcp_sample_check(out, lits, off, n, tl, to, cap, k=64):
+def bcp_sample_check(out, lits, off, n, tl, to, cap, k=64, strategy="watched"):
     """Compares k evenly spaced trails of the last timed launch's outputs with
     the oracle, bit for bit (status, conflict clause, stop index, implied
     literals and reasons in order, counters); raises on a difference."""
@@ -446,7 +454,8 @@ def bcp_sample_check(out, lits, off, n, tl, to, cap, k=64):
     sub_to = np.zeros(len(idx) + 1, np.int64)
     sub_to[1:] = np.cumsum(to[idx + 1] - to[idx])
     sub_tl = np.concatenate([tl[to[i]:to[i + 1]] for i in idx])
-    ref = oracle.BCPOracle(lits, off, n).run(sub_tl, sub_to, impl_cap=cap, threads=os.cpu_count() or 1)
+    ref = oracle.BCPOracle(lits, off, n).run(sub_tl, sub_to, impl_cap=cap, threads=os.cpu_count() or 1,
+                                             strategy=strategy)
     got = {key: out[key].cpu().numpy()[idx] for key in ("status", "conflict", "stop", "n_impl", "counters")}
     for key in ("status", "conflict", "stop", "n_impl", "counters"):
         if not np.array_equal(got[key], ref[key]):
@@ -459,7 +468,124 @@ def bcp_sample_check(out, lits, off, n, tl, to, cap, k=64):
                 np.array_equal(ir[j, :kk], ref["impl_reason"][j, :kk])):
             raise AssertionError(f"bench check: implications of trail {int(idx[j])} differ from the oracle")
     return {"trails": int(len(idx)), "bit_exact": True, "against": "oracle/bcp_ref.c",
-            "propagations": int(ref["counters"][:, 0].sum())}
+            "units": int(ref["counters"][:, 1 if strategy == "full_scan" else 0].sum())}
+
+
+# ---------------------------------------------------------------- full-scan strategy
+SCAN_METRIC = "full-scan clause evaluations/s"
+SCAN_UNIT = "evaluations/s"
+
+
+def run_scan_gpu(args):
+    """The BCP workload's trails under the reference's full-scan clause
+    evaluation (BASIC_SEARCH): every trail literal assigned, then sweeps over
+    all clauses in index order until a sweep adds nothing or a clause is
+    false.  value = clause evaluations/s (device time, inputs in HBM)."""
+    import torch
+    import gpupsat_gb300 as g
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda:0")
+    n, m, lits, off, tl, to = workload(args, 0)
+    T, cap = args.trails, args.impl_cap
+    f = g.Formula(lits, off, n)
+    b = g.BCPBatch(f, impl_cap=cap, max_slots=args.slots or 0)
+    b.set_strategy("full_scan")
+    d_tl, d_to = torch.from_numpy(tl).to(dev), torch.from_numpy(to).to(dev)
+    out = dict(status=torch.empty(T, dtype=torch.int32, device=dev),
+               conflict=torch.empty(T, dtype=torch.int32, device=dev),
+               stop=torch.empty(T, dtype=torch.int32, device=dev),
+               n_impl=torch.empty(T, dtype=torch.int64, device=dev),
+               impl_lit=torch.empty(T, cap, dtype=torch.int32, device=dev),
+               impl_reason=torch.empty(T, cap, dtype=torch.int32, device=dev),
+               counters=torch.empty(T, 6, dtype=torch.int64, device=dev))
+    stream = torch.cuda.Stream(device=dev)
+    for _ in range(args.warmup):
+        b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
+    stream.synchronize()
+    cnt = out["counters"].cpu().numpy()
+    evals_step = int(cnt[:, 1].sum())
+    bytes_step = alg_bytes(cnt)
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        b.run_device(d_tl, d_to, out, stream=stream.cuda_stream)
+        evs[i + 1].record(stream)
+    stream.synchronize()
+    clk = clocks.stop()
+    elapsed = sum(evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)) / 1000.0
+    assert int(out["counters"][:, 1].sum().item()) == evals_step, "evaluation count changed between steps"
+    e2e = None
+    if not args.no_e2e:
+        h_out = b.host_outputs(T, counters=True)
+        b.run_host(tl, to, out=h_out)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b.run_host(tl, to, out=h_out)
+        e2e_s = time.perf_counter() - t0
+        maxn = int(h_out["n_impl"].max())
+        d2h = T * (4 * 3 + 8 + 8 * 6) + 2 * 4 * T * min(maxn, cap)
+        e2e = {"value": evals_step * args.steps / e2e_s, "unit": SCAN_UNIT,
+               "h2d_bytes_per_step": int(tl.nbytes + to.nbytes), "d2h_bytes_per_step": int(d2h)}
+    peak, peak_src = peaks()
+    achieved = bytes_step / (elapsed / args.steps) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, units, dt, Tc = cpu_baseline(lits, off, n, tl, to, args.cpu_trails, threads, strategy="full_scan")
+        cpu = {"value": v, "unit": SCAN_UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {Tc} of the {T} trails ({units} clause evaluations, {dt:.2f} s); oracle/bcp_ref.c "
+                         f"full-scan restatement (pinned to the reference's own full-scan propagation)"}
+    check = bcp_sample_check(out, lits, off, n, tl, to, cap, strategy="full_scan")
+    line = {"metric": SCAN_METRIC, "value": evals_step * args.steps / elapsed, "unit": SCAN_UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
+            "config": dict(config(args, n, m), workload="BCP trails under the reference's full-scan clause "
+                                                        "evaluation (BASIC_SEARCH)",
+                           l2="formula resident in L2 up to n of about 2e6; the assignment bits in shared "
+                              "memory up to n = 196,608"),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_src, "alg_bytes_per_launch": bytes_step,
+                         "kernel": "gpsat::bcp::scan_kernel"},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": args.steps * (4 if T > 1 else 1),
+            "sweeps_per_step": int(cnt[:, 0].sum()), "check": check}
+    print(json.dumps(line))
+    b.close()
+    f.close()
+
+
+def run_scan_reference(args):
+    """Reference arm of the full-scan workload: the oracle's restatement on
+    all host cores over the same trails (the reference's own full-scan
+    propagation is host-built only at small n in the tests)."""
+    import oracle
+    n, m, lits, off, tl, to = workload(args, 0, gen=oracle)
+    threads = os.cpu_count() or 1
+    per_step = max(16, min(args.cpu_trails, args.trails))
+    vals = []
+    for s in range(args.warmup + args.steps):
+        b = (s * per_step) % max(1, args.trails - per_step + 1)
+        sub_to = to[b:b + per_step + 1] - to[b]
+        sub_tl = tl[to[b]:to[b + per_step]]
+        v, units, dt, T = cpu_baseline(lits, off, n, sub_tl, sub_to, per_step, threads, strategy="full_scan")
+        if s >= args.warmup:
+            vals.append((units, dt))
+    value = sum(u for u, _ in vals) / sum(d for _, d in vals)
+    print(json.dumps({"impl": "reference", "metric": SCAN_METRIC, "value": value, "unit": SCAN_UNIT,
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1000 * sum(d for _, d in vals) / len(vals), "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+                      "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
+                      "config": dict(config(args, n, m), workload="BCP trails under the reference's full-scan "
+                                                                  "clause evaluation (BASIC_SEARCH)",
+                                     l2="host run"),
+                      "cpu_baseline": {"value": value, "unit": SCAN_UNIT, "cores": threads, "kind": "port",
+                                       "sample": f"{per_step} trails per step of the same workload"},
+                      "e2e": {"value": value, "unit": SCAN_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
 # ---------------------------------------------------------------- batched solving
@@ -941,6 +1067,11 @@ def main():
             run_solve_reference(args)
         else:
             run_solve_gpu(args)
+    elif args.workload == "full_scan":
+        if args.impl == "reference":
+            run_scan_reference(args)
+        else:
+            run_scan_gpu(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

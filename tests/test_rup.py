@@ -123,6 +123,17 @@ def test_rup_rejects_any_proof_of_a_satisfiable_formula(gpsat):
     assert sat
     ok, step = gpsat.check_rup(lits, off, 30, np.zeros(0, np.int32))
     assert not ok and step == 0
+    # random logs (units, binaries, ternaries, the empty clause last) never refute it
+    rng = np.random.default_rng(11)
+    for _ in range(200):
+        log = []
+        for _ in range(int(rng.integers(1, 12))):
+            k = int(rng.integers(1, 4))
+            vs = rng.choice(30, size=k, replace=False) + 1
+            log.append([int(v) * int(rng.choice([-1, 1])) for v in vs])
+        log.append([])
+        ok, _ = gpsat.check_rup(lits, off, 30, flat(log))
+        assert not ok
 
 
 def test_rup_with_assumptions(gpsat):
