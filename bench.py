@@ -186,14 +186,14 @@ def peaks():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def traffic_per_launch(n, trails):
+def traffic_per_launch(n, trails, window, slots):
     """DRAM bytes of one launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)
-    from the committed capture of this exact workload, else None."""
+    from the committed capture of this exact workload and launch shape, else None."""
     p = ROOT / "profiles" / "bcp_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    if d.get("n_vars") != n or d.get("n_trails") != trails:
+    if (d.get("n_vars"), d.get("n_trails"), d.get("window"), d.get("slots")) != (n, trails, window, slots):
         return None
     return d["dram_bytes_per_launch"]
 
@@ -409,7 +409,7 @@ def run_gpu(args):
     avg_launch_s = elapsed / args.steps
     achieved = bytes_step / avg_launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic_per_launch(n, T), "peak_source": peak_src,
+            "traffic": traffic_per_launch(n, T, b.window, active), "peak_source": peak_src,
             "alg_bytes_per_launch": bytes_step, "kernel": f"gpsat::bcp::w{b.window // 32}::bcp_kernel"}
     cpu = None
     if not args.no_cpu:
@@ -1047,8 +1047,8 @@ def main():
     args = parse()
     if args.instances is None:
         args.instances = {"planted": 128, "seeding": 1024}.get(args.workload, 16384)
-    if args.workload == "solve" and args.steps == 20:
-        args.steps = 1    # one batch solve is about 20 s
+    if args.workload in ("solve", "planted") and args.steps == 20:
+        args.steps = 1    # one batch solve is about 20 s (planted 1,024 instances: about 50 s)
     if args.workload == "seeding":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned seeding; its "
