@@ -119,6 +119,22 @@ __device__ __forceinline__ int block_min(Smem &sm, int v)
     return sm.key_min;
 }
 
+// one 32-byte list entry in one 256-bit load (entries are 32-byte aligned:
+// the formula's and each slot's arrays start on 256-byte boundaries); the
+// formula's entries through the non-coherent path
+__device__ __forceinline__ void ld_entry(const int4 *p, int4 &a, int4 &b)
+{
+    asm volatile("ld.global.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+                 : "l"(p));
+}
+__device__ __forceinline__ void ld_entry_nc(const int4 *p, int4 &a, int4 &b)
+{
+    asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+                 : "l"(p));
+}
+
 __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slot)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -299,9 +315,10 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
                 int32_t p = cur_dp;
                 int k = 0;
                 while (p >= 0 && k < W) {
-                    const int4 a = arena[2 * p];
+                    int4 a, a2;
+                    ld_entry(arena + 2 * p, a, a2);
                     sm.dyn0[k] = a;
-                    sm.dyn1[k] = arena[2 * p + 1];
+                    sm.dyn1[k] = a2;
                     p = a.w;
                     sm.dyn_next[k] = p;
                     k++;
@@ -390,21 +407,18 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
                     el = sm.dyn1[tid];
                 } else {
                     const size_t w = cur_wk + (uint32_t)(tid - ndyn);
-                    en = d.w0ent[2 * w];
-                    el = d.w0ent[2 * w + 1];
+                    ld_entry_nc(d.w0ent + 2 * w, en, el);
                 }
             } else {
                 my_scan = sm.pos_scan[tid];
                 const int q = tid - sm.sc_b[my_scan];
                 const int32_t head = sm.sc_head[my_scan];
                 if (head >= 0 && q == 0) {
-                    en = arena[2 * head];
-                    el = arena[2 * head + 1];
+                    ld_entry(arena + 2 * head, en, el);
                     sm.sc_next[my_scan] = en.w;
                 } else {
                     const size_t w = sm.sc_wk[my_scan] + (uint32_t)(q - (head >= 0 ? 1 : 0));
-                    en = d.w0ent[2 * w];
-                    el = d.w0ent[2 * w + 1];
+                    ld_entry_nc(d.w0ent + 2 * w, en, el);
                 }
             }
         }
