@@ -77,6 +77,9 @@ def parse():
                     help="bcp: trails in flight (default: the autotuner's choice, timed on warm-up launches)")
     ap.add_argument("--arena-cap", type=int, default=0,
                     help="bcp: added watch entries per trail slot (default: the library's, 2^17)")
+    ap.add_argument("--order-pivot", type=int, default=None,
+                    help="bcp: trails whose literal count is nearest this start first (default: the autotuner's "
+                         "choice; 0 = shortest first)")
     ap.add_argument("--window", type=int, default=None, choices=[64, 128, 256],
                     help="bcp: watch entries per round and trail (default: the autotuner's choice); with "
                          "--slots, no tuning launch runs")
@@ -350,10 +353,13 @@ def run_gpu(args):
     # depend on them)
     if args.slots is None:
         windows = (args.window,) if args.window is not None else (128, 256, 64)
-        tuning = b.tune(d_tl, d_to, out, stream.cuda_stream, windows=windows)
+        pivots = (0.0, 0.1, 0.2, 0.3, 0.4) if args.order_pivot is None else ()
+        tuning = b.tune(d_tl, d_to, out, stream.cuda_stream, windows=windows, pivots=pivots)
     else:
         b.set_active_slots(args.slots)
         tuning = None
+    if args.order_pivot is not None:
+        b.set_order_pivot(args.order_pivot)
     active = b.active or b.window_slots(b.window)
     cnt = out["counters"].cpu().numpy()
     props_step = int(cnt[:, 0].sum())
@@ -424,10 +430,11 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded uniform random 3-SAT and seeded partial trails",
             "config": config(args, n, m),
-            "launch": {"window": b.window, "threads_per_trail": b.window, "slots": active,
-                       "tuning_ms": {f"{w}x{n}": round(v, 3) for (w, n), v in tuning.items()} if tuning else None},
+            "launch": {"window": b.window, "threads_per_trail": b.window, "slots": active, "order_pivot": b.pivot,
+                       "tuning_ms": {f"{w}x{n}/{p}": round(v, 3) for (w, n, p), v in tuning.items()} if tuning else None},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps * (4 if T > active else 1),  # order kernels + BCP kernel
+            # trail application + (order kernels when more trails than slots) + BCP kernel
+            "gpu_launches": args.steps * (5 if T > active else 2),
             "kernel": f"gpsat::bcp::w{b.window // 32}::bcp_kernel",
             "props_per_step": props_step, "conflicts_per_step": int((out["status"] == 1).sum().item()),
             "check": check}

@@ -79,6 +79,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gpsat_bcp_set_active_slots": (ctypes.c_int, [_vp, ctypes.c_int32]),
         "gpsat_bcp_set_strategy": (ctypes.c_int, [_vp, ctypes.c_int32]),
         "gpsat_bcp_set_window": (ctypes.c_int, [_vp, ctypes.c_int32]),
+        "gpsat_bcp_set_order_pivot": (ctypes.c_int, [_vp, ctypes.c_int64]),
         "gpsat_bcp_window_slots": (ctypes.c_int, [_vp, ctypes.c_int32, _c_i32p]),
         "gpsat_bcp_run_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 8),
         "gpsat_bcp_run_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32] + [_vp] * 7),
@@ -261,6 +262,7 @@ class BCPBatch:
         self._h = _vp()
         check(lib().gpsat_bcp_create(formula.handle, max_slots, impl_cap, arena_cap, ctypes.byref(self._h)))
         self.active = 0
+        self.pivot = 0
         self.window = 128
         self.strategy = "watched"
 
@@ -282,16 +284,29 @@ class BCPBatch:
         self.window = int(entries)
 
     def tune(self, trail_lits, trail_offsets, out: dict, stream: int, windows=(128, 256, 64),
-             fractions=(1.0, 0.75, 0.5)):
+             fractions=(1.0, 0.75, 0.5), pivots=(0.0, 0.1, 0.2, 0.3, 0.4)):
         """The BCP autotuner: times one run_device launch of these trails (after
         one untimed launch) for every window width and, at each width, every
-        fraction of the slots that width keeps resident; keeps the fastest
-        pair.  Returns {(window, active slots): ms}.  Outputs do not depend on
+        fraction of the slots that width keeps resident, then, at the fastest
+        pair, the processing order's pivot at each quantile of the trail
+        lengths in `pivots` (0: shortest first); keeps the fastest setting.
+        Returns {(window, active slots, pivot): ms}.  Outputs do not depend on
         the setting; `out` holds the last launch's results."""
         import torch
         st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
         slots = self.info()["slots"]
         times = {}
+
+        def timed(key):
+            self.run_device(trail_lits, trail_offsets, out, stream=stream)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            self.run_device(trail_lits, trail_offsets, out, stream=stream)
+            b.record(st)
+            b.synchronize()
+            times[key] = a.elapsed_time(b)
+
+        self.set_order_pivot(0)
         for w in windows:
             self.set_window(w)
             per = self.window_slots(w)
@@ -300,17 +315,29 @@ class BCPBatch:
                 if n > slots:
                     continue
                 self.set_active_slots(n)
-                self.run_device(trail_lits, trail_offsets, out, stream=stream)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(st)
-                self.run_device(trail_lits, trail_offsets, out, stream=stream)
-                b.record(st)
-                b.synchronize()
-                times[(w, n)] = a.elapsed_time(b)
-        (w, n) = min(times, key=times.get)
+                timed((w, n, 0))
+        (w, n, _) = min(times, key=times.get)
         self.set_window(w)
         self.set_active_slots(n)
+        offs = trail_offsets.cpu().numpy() if hasattr(trail_offsets, "cpu") else np.asarray(trail_offsets)
+        lens = np.diff(offs.astype(np.int64))
+        for q in pivots:
+            p = int(np.quantile(lens, q)) if q > 0 and len(lens) else 0
+            if p == 0 or (w, n, p) in times:
+                continue
+            self.set_order_pivot(p)
+            timed((w, n, p))
+        (w, n, p) = min(times, key=times.get)
+        self.set_window(w)
+        self.set_active_slots(n)
+        self.set_order_pivot(p)
         return times
+
+    def set_order_pivot(self, pivot: int) -> None:
+        """Later runs start the trails whose literal count is nearest `pivot`
+        first (0: shortest first); outputs do not depend on it."""
+        check(lib().gpsat_bcp_set_order_pivot(self._h, int(pivot)))
+        self.pivot = int(pivot)
 
     def set_strategy(self, strategy: str) -> None:
         """"watched" (two watched literals, the default) or "full_scan" (the

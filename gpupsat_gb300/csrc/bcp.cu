@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstddef>
 #include <cstdio>
@@ -28,26 +29,33 @@ const Variant *variant(int warps)
 }
 
 // ---------------------------------------------------------------------------
-// Processing order: shortest trails first.  A launch lasts as long as its
-// slowest trail, and when there are more trails than resident warps the
-// last ones start only as others finish.  The trails that propagate longest
-// are those that reach their fixpoint without a conflict, and a trail that
-// assigns fewer variables is the more likely to: starting the short ones
-// first starts the long-running ones at once.  (Outputs do not depend on the
-// order; at the 4096-trail benchmark shape the measured per-trail durations
-// give a 37.9 ms schedule instead of 41.4 ms.)  A counting sort on length / 16.
+// Processing order.  A launch lasts as long as its slowest trail, and when
+// there are more trails than resident blocks the last ones start only as
+// others finish, so the long-running trails should start first.  The trails
+// that propagate longest are those that reach their fixpoint without a
+// conflict: a trail that assigns fewer variables is the more likely to, but
+// it also has fewer literals to propagate, so the longest ones assign a
+// middling number.  The order therefore takes the trails whose length is
+// nearest a pivot first (pivot 0: shortest first), and the pivot is tuned on
+// the caller's trails (BCPBatch.tune).  (Outputs do not depend on the order.
+// At the 4096-trail benchmark shape, the measured per-trail durations of one
+// launch give an 18.5 ms list schedule shortest first and 15.0-15.4 ms with
+// the pivot at the 25th-30th percentile of the lengths.)  A counting sort on
+// |length - pivot| / 16.
 constexpr int ORDER_BUCKETS = 4096;
 
-__device__ __forceinline__ int order_bucket(const int64_t *toff, int t)
+__device__ __forceinline__ int order_bucket(const int64_t *toff, int t, int64_t pivot)
 {
-    const int64_t len = toff[t + 1] - toff[t];
-    return len <= 0 ? 0 : (int)(len >> 4 < ORDER_BUCKETS - 1 ? len >> 4 : ORDER_BUCKETS - 1);
+    int64_t len = toff[t + 1] - toff[t];
+    if (len < 0) len = 0;
+    const int64_t dist = len >= pivot ? len - pivot : pivot - len;
+    return (int)(dist >> 4 < ORDER_BUCKETS - 1 ? dist >> 4 : ORDER_BUCKETS - 1);
 }
 
-__global__ void order_count(const int64_t *toff, int T, unsigned *hist)
+__global__ void order_count(const int64_t *toff, int T, int64_t pivot, unsigned *hist)
 {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
-        atomicAdd(&hist[order_bucket(toff, t)], 1u);
+        atomicAdd(&hist[order_bucket(toff, t, pivot)], 1u);
 }
 
 // one block of 1024 threads: the counts become exclusive prefix sums in place
@@ -77,10 +85,80 @@ __global__ void __launch_bounds__(1024) order_scan(unsigned *hist)
     }
 }
 
-__global__ void order_scatter(const int64_t *toff, int T, unsigned *hist, int32_t *order)
+__global__ void order_scatter(const int64_t *toff, int T, int64_t pivot, unsigned *hist, int32_t *order)
 {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
-        order[atomicAdd(&hist[order_bucket(toff, t)], 1u)] = t;
+        order[atomicAdd(&hist[order_bucket(toff, t, pivot)], 1u)] = t;
+}
+
+// ---------------------------------------------------------------------------
+// Trail application ahead of the BCP kernel.  The reference assigns every
+// trail literal before it propagates any (SATSolver/VariablesStateHandler.cu
+// :35-59), so the assignment words of all the launch's trails can be built
+// at once, in parallel over the whole GPU, instead of by each trail's block
+// (one dependent global atomic per literal) before its rounds start.  A block
+// builds one trail's words at a time in shared memory, a chunk of variables
+// per pass over the trail's literals, and writes every word of the chunk out
+// (so the words need no clearing between launches: each launch writes them
+// all).  A literal out of range, or a variable given both signs, marks the
+// trail bad (the BCP kernel then reports GPSAT_BCP_BAD_TRAIL for it).
+constexpr int APPLY_NT = 512;
+constexpr int APPLY_CHUNK_WORDS = 16384;   // 64 KB: 262,144 variables per pass
+constexpr int64_t APPLY_MAX_BYTES = int64_t(8) << 30;   // above this the blocks assign their own trails
+
+__global__ void __launch_bounds__(APPLY_NT) apply_kernel(const int32_t *__restrict__ trail,
+                                                        const int64_t *__restrict__ toff, int32_t n_trails,
+                                                        int32_t n, int64_t n_words, uint32_t *__restrict__ tasg,
+                                                        int32_t *__restrict__ tbad)
+{
+    extern __shared__ uint32_t chunk[];   // APPLY_CHUNK_WORDS words
+    __shared__ int s_bad;
+    for (int t = blockIdx.x; t < n_trails; t += gridDim.x) {
+        const int64_t tb = toff[t], tn = toff[t + 1] - tb;
+        uint32_t *out = tasg + (size_t)t * n_words;
+        if (threadIdx.x == 0) s_bad = tn < 0;
+        for (int64_t w0 = 0; w0 < n_words; w0 += APPLY_CHUNK_WORDS) {
+            const int cw = (int)(n_words - w0 < APPLY_CHUNK_WORDS ? n_words - w0 : APPLY_CHUNK_WORDS);
+            for (int i = threadIdx.x; i < cw; i += APPLY_NT) chunk[i] = 0u;
+            __syncthreads();
+            const int64_t v_lo = w0 * 16, v_hi = (w0 + cw) * 16;
+            bool bad = false;
+#pragma unroll 4
+            for (int64_t i = threadIdx.x; i < tn; i += APPLY_NT) {
+                const int32_t x = trail[tb + i];
+                if (x == 0 || x > n || x < -n) {
+                    bad = true;
+                    continue;
+                }
+                const int32_t v = (x > 0 ? x : -x) - 1;
+                if (v < v_lo || v >= v_hi) continue;
+                const int sh = (v & 15) << 1;
+                const uint32_t bits = (x > 0 ? 3u : 1u) << sh;
+                const uint32_t old = atomicOr(&chunk[(v >> 4) - w0], bits);
+                if (((old >> sh) & 1u) && (((old ^ bits) >> sh) & 2u)) bad = true;
+            }
+            if (bad) s_bad = 1;   // every writer writes 1
+            __syncthreads();
+            for (int i = threadIdx.x; i < cw; i += APPLY_NT) out[w0 + i] = chunk[i];
+            __syncthreads();   // the chunk is read out before the next pass clears it
+        }
+        if (threadIdx.x == 0) tbad[t] = s_bad;
+        __syncthreads();       // s_bad is read before the next trail resets it
+    }
+}
+
+// the 64 KB of dynamic shared memory needs the opt-in, once per device
+cudaError_t apply_allow()
+{
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, APPLY_CHUNK_WORDS * 4);
+    if (e == cudaSuccess) done.fetch_or(bit);
+    return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -310,6 +388,7 @@ struct gpsat_bcp {
     int device = 0;
     int32_t slots = 0;
     int32_t active = 0;                // slots the launches use (0: all)
+    int64_t pivot = 0;                 // processing order: trail lengths nearest this first
     int32_t strategy = GPSAT_BCP_WATCHED;
     int32_t warps = bcp::DEFAULT_WARPS;    // window width of the two-watched-literal kernel / 32
     int32_t resident[bcp::MAX_WARPS + 1] = {};   // per width: blocks the GPU keeps resident
@@ -330,6 +409,11 @@ struct gpsat_bcp {
     int64_t trail_cap = 0, toff_cap = 0;
     void *d_out = nullptr;
     int64_t out_cap = 0;
+    // trails applied ahead of the BCP kernel (apply_kernel)
+    uint32_t *tasg = nullptr;
+    int32_t *tbad = nullptr;
+    int64_t tasg_cap = 0, tbad_cap = 0;   // words, trails
+    int32_t apply_blocks = 0;             // resident blocks of apply_kernel (0: not looked up yet)
 };
 
 namespace {
@@ -349,6 +433,55 @@ void bcp_free(gpsat_bcp *b)
     cudaFree(b->d_trail);
     cudaFree(b->d_toff);
     cudaFree(b->d_out);
+    cudaFree(b->tasg);
+    cudaFree(b->tbad);
+}
+
+// Trail t's assignment words built ahead of the BCP kernel into tasg (grown
+// on demand); false when they would take more than APPLY_MAX_BYTES or cannot
+// be allocated, and the BCP kernel's blocks then assign their own trails.
+bool apply_trails(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, cudaStream_t st)
+{
+    const int64_t words = (int64_t)n_trails * b->n_words;
+    if (n_trails <= 0 || words * 4 > bcp::APPLY_MAX_BYTES) return false;
+    if (words > b->tasg_cap) {
+        cudaFree(b->tasg);
+        b->tasg = nullptr;
+        b->tasg_cap = 0;
+        if (cudaMalloc(&b->tasg, (size_t)words * 4) != cudaSuccess) {
+            cudaGetLastError();
+            b->tasg = nullptr;
+            return false;
+        }
+        b->tasg_cap = words;
+    }
+    if (n_trails > b->tbad_cap) {
+        cudaFree(b->tbad);
+        b->tbad = nullptr;
+        b->tbad_cap = 0;
+        if (cudaMalloc(&b->tbad, (size_t)n_trails * 4) != cudaSuccess) {
+            cudaGetLastError();
+            b->tbad = nullptr;
+            return false;
+        }
+        b->tbad_cap = n_trails;
+    }
+    if (bcp::apply_allow() != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (b->apply_blocks == 0) {
+        int per_sm = 0, sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bcp::apply_kernel, bcp::APPLY_NT,
+                                                          bcp::APPLY_CHUNK_WORDS * 4) != cudaSuccess)
+            cudaGetLastError();
+        b->apply_blocks = std::max(1, sms * std::max(per_sm, 1));
+    }
+    const int grid = std::min<int32_t>(n_trails, b->apply_blocks);
+    bcp::apply_kernel<<<grid, bcp::APPLY_NT, bcp::APPLY_CHUNK_WORDS * 4, st>>>(trail, toff, n_trails, b->f->h.n_vars,
+                                                                               b->n_words, b->tasg, b->tbad);
+    return cudaGetLastError() == cudaSuccess;
 }
 
 int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, int32_t *status,
@@ -356,7 +489,7 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
            cudaStream_t st)
 {
     const gpsat_formula *f = b->f;
-    bcp::Dev d;
+    bcp::Dev d{};
     d.n_vars = f->h.n_vars;
     d.n_clauses = (int32_t)f->h.n_clauses();
     d.lits = f->d_lits;
@@ -412,9 +545,9 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
         err = cudaMemsetAsync(b->hist, 0, bcp::ORDER_BUCKETS * sizeof(unsigned), st);
         if (err != cudaSuccess) return cuda_error(err, "bcp order reset");
         const int g = std::min(1024, (n_trails + 255) / 256);
-        bcp::order_count<<<g, 256, 0, st>>>(toff, n_trails, b->hist);
+        bcp::order_count<<<g, 256, 0, st>>>(toff, n_trails, b->pivot, b->hist);
         bcp::order_scan<<<1, 1024, 0, st>>>(b->hist);
-        bcp::order_scatter<<<g, 256, 0, st>>>(toff, n_trails, b->hist, b->order);
+        bcp::order_scatter<<<g, 256, 0, st>>>(toff, n_trails, b->pivot, b->hist, b->order);
         d.order = b->order;
     }
     if (scan) {
@@ -425,6 +558,10 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
             bcp::scan_kernel<false><<<d.n_slots, bcp::SCAN_NT, 0, st>>>(d, f->d_coff);
         err = cudaGetLastError();
     } else {
+        if (apply_trails(b, trail, toff, n_trails, st)) {
+            d.tasg = b->tasg;
+            d.tbad = b->tbad;
+        }
         err = bcp::variant(b->warps)->launch(d, d.n_slots, st);
     }
     if (err != cudaSuccess) return cuda_error(err, "bcp kernel launch");
@@ -531,6 +668,14 @@ extern "C" int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n)
     return GPSAT_OK;
 }
 
+extern "C" int gpsat_bcp_set_order_pivot(gpsat_bcp *b, int64_t pivot)
+{
+    if (!b) return set_error(GPSAT_ERR_ARG, "gpsat_bcp_set_order_pivot: null handle");
+    if (pivot < 0) return set_error(GPSAT_ERR_ARG, "gpsat_bcp_set_order_pivot: negative pivot");
+    b->pivot = pivot;
+    return GPSAT_OK;
+}
+
 extern "C" int gpsat_bcp_set_window(gpsat_bcp *b, int32_t entries)
 {
     if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
@@ -572,46 +717,13 @@ extern "C" int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, con
                   impl_reason, counters, (cudaStream_t)stream);
 }
 
-extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
-                                  int32_t n_trails, int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
-                                  int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
+namespace {
+// The trails copied into the handle's staging buffers (grown on demand) on
+// stream st: device memory that apply_kernel can pass over more than once.
+int stage_trails(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails,
+                 cudaStream_t st)
 {
-    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index ||
-                                                !n_impl || !impl_lit || !impl_reason)))
-        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_host: bad argument");
-    if (n_trails == 0) return GPSAT_OK;
-    cudaError_t err = cudaSetDevice(b->device);
-    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
     const int64_t nl = trail_offsets[n_trails];
-    if (nl < 0 || (nl > 0 && !trail_lits)) return set_error(GPSAT_ERR_ARG, "bad trail offsets");
-    {
-        // Every buffer page-locked (cudaHostAlloc / cudaHostRegister, as
-        // torch's pin_memory): the kernel reads the trails and writes the
-        // results in place, over the CPU-GPU link, with no staging copies.
-        const void *hp[9] = {nl > 0 ? (const void *)trail_lits : (const void *)trail_offsets, trail_offsets, status, conflict_clause, stop_index,
-                             n_impl, impl_lit, impl_reason, counters ? (const void *)counters : trail_offsets};
-        void *dp[9];
-        bool all = true;
-        for (int i = 0; i < 9 && all; i++) {
-            cudaPointerAttributes a;
-            if (cudaPointerGetAttributes(&a, hp[i]) != cudaSuccess) {
-                cudaGetLastError();
-                all = false;
-            } else {
-                all = a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
-                dp[i] = a.devicePointer;
-            }
-        }
-        if (all) {
-            int rc = launch(b, (const int32_t *)dp[0], (const int64_t *)dp[1], n_trails, (int32_t *)dp[2],
-                            (int32_t *)dp[3], (int32_t *)dp[4], (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7],
-                            counters ? (int64_t *)dp[8] : nullptr, 0);
-            if (rc != GPSAT_OK) return rc;
-            err = cudaStreamSynchronize(0);
-            if (err != cudaSuccess) return cuda_error(err, "bcp run");
-            return GPSAT_OK;
-        }
-    }
     if (nl > b->trail_cap) {
         cudaFree(b->d_trail);
         b->d_trail = nullptr;
@@ -630,6 +742,60 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
         }
         b->toff_cap = n_trails + 1;
     }
+    if (nl > 0 && cudaMemcpyAsync(b->d_trail, trail_lits, nl * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return cuda_error(cudaGetLastError(), "trail copy");
+    if (cudaMemcpyAsync(b->d_toff, trail_offsets, (int64_t)(n_trails + 1) * 8, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+        return cuda_error(cudaGetLastError(), "offset copy");
+    return GPSAT_OK;
+}
+}  // namespace
+
+extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
+                                  int32_t n_trails, int32_t *status, int32_t *conflict_clause, int32_t *stop_index,
+                                  int64_t *n_impl, int32_t *impl_lit, int32_t *impl_reason, int64_t *counters)
+{
+    if (!b || n_trails < 0 || (n_trails > 0 && (!trail_offsets || !status || !conflict_clause || !stop_index ||
+                                                !n_impl || !impl_lit || !impl_reason)))
+        return set_error(GPSAT_ERR_ARG, "gpsat_bcp_run_host: bad argument");
+    if (n_trails == 0) return GPSAT_OK;
+    cudaError_t err = cudaSetDevice(b->device);
+    if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
+    const int64_t nl = trail_offsets[n_trails];
+    if (nl < 0 || (nl > 0 && !trail_lits)) return set_error(GPSAT_ERR_ARG, "bad trail offsets");
+    {
+        // Every buffer page-locked (cudaHostAlloc / cudaHostRegister, as
+        // torch's pin_memory): the trails are copied to the device by DMA
+        // (the trail-application kernel passes over them more than once) and
+        // the kernel writes the results in place, over the CPU-GPU link, with
+        // no staging copies.
+        const void *hp[9] = {nl > 0 ? (const void *)trail_lits : (const void *)trail_offsets, trail_offsets, status, conflict_clause, stop_index,
+                             n_impl, impl_lit, impl_reason, counters ? (const void *)counters : trail_offsets};
+        void *dp[9];
+        bool all = true;
+        for (int i = 0; i < 9 && all; i++) {
+            cudaPointerAttributes a;
+            if (cudaPointerGetAttributes(&a, hp[i]) != cudaSuccess) {
+                cudaGetLastError();
+                all = false;
+            } else {
+                all = a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+                dp[i] = a.devicePointer;
+            }
+        }
+        if (all) {
+            int rc = stage_trails(b, trail_lits, trail_offsets, n_trails, 0);
+            if (rc != GPSAT_OK) return rc;
+            rc = launch(b, b->d_trail, b->d_toff, n_trails, (int32_t *)dp[2], (int32_t *)dp[3], (int32_t *)dp[4],
+                        (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7], counters ? (int64_t *)dp[8] : nullptr, 0);
+            if (rc != GPSAT_OK) return rc;
+            err = cudaStreamSynchronize(0);
+            if (err != cudaSuccess) return cuda_error(err, "bcp run");
+            return GPSAT_OK;
+        }
+    }
+    int rc = stage_trails(b, trail_lits, trail_offsets, n_trails, 0);
+    if (rc != GPSAT_OK) return rc;
     const int64_t T = n_trails;
     const int64_t need = T * (4 + 4 + 4 + 8 + 8 * GPSAT_BCP_NCOUNTERS) + 2 * T * b->impl_cap * 4 + 64;
     if (need > b->out_cap) {
@@ -656,12 +822,8 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
     p += T * b->impl_cap * 4;
     int32_t *d_ireason = (int32_t *)p;
     cudaStream_t st = 0;
-    if (nl > 0 && cudaMemcpyAsync(b->d_trail, trail_lits, nl * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return cuda_error(cudaGetLastError(), "trail copy");
-    if (cudaMemcpyAsync(b->d_toff, trail_offsets, (T + 1) * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return cuda_error(cudaGetLastError(), "offset copy");
-    int rc = launch(b, b->d_trail, b->d_toff, n_trails, d_status, d_confl, d_stop, d_nimpl, d_ilit, d_ireason,
-                    counters ? d_cnt : nullptr, st);
+    rc = launch(b, b->d_trail, b->d_toff, n_trails, d_status, d_confl, d_stop, d_nimpl, d_ilit, d_ireason,
+                counters ? d_cnt : nullptr, st);
     if (rc != GPSAT_OK) return rc;
     bool ok = cudaMemcpyAsync(status, d_status, T * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
               cudaMemcpyAsync(conflict_clause, d_confl, T * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
@@ -854,7 +1016,7 @@ extern "C" int gpsat_bcp_run_static(const gpsat_formula *f, int64_t impl_cap, in
     if (err != cudaSuccess) return cuda_error(err, "gpsat_bcp_run_static: clearing the static scratch");
     if (n_trails == 0) return GPSAT_OK;
 
-    bcp::Dev d;
+    bcp::Dev d{};
     d.n_vars = f->h.n_vars;
     d.n_clauses = (int32_t)f->h.n_clauses();
     d.lits = f->d_lits;

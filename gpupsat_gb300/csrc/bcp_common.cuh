@@ -55,6 +55,11 @@ struct Dev {
     int64_t *nimpl;
     int32_t *ilit, *ireason;
     int64_t *counters;
+    // trails applied beforehand (apply_kernel): trail t's assignment words at
+    // tasg + t * n_words and its bad-trail flag tbad[t]; null: each block
+    // assigns its trail into its slot's asg words and clears them after
+    uint32_t *tasg;
+    const int32_t *tbad;
 };
 
 __device__ __forceinline__ unsigned lanemask_lt()

@@ -138,7 +138,8 @@ __device__ __forceinline__ void ld_entry_nc(const int4 *p, int4 &a, int4 &b)
 __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slot)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint32_t *asg = d.asg + (size_t)slot * d.n_words;
+    const bool pre = d.tasg != nullptr;   // the trail was assigned by apply_kernel
+    uint32_t *asg = pre ? d.tasg + (size_t)t * d.n_words : d.asg + (size_t)slot * d.n_words;
     uint32_t *dh = d.dh + (size_t)slot * d.n_pad;
     uint32_t *cst = d.cst + (size_t)slot * d.m_pad;
     int4 *arena = d.arena + (size_t)slot * d.arena_cap * 2;
@@ -166,9 +167,9 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
 
     // ---- assign every trail literal first: an atomic OR of its two bits; the
     // old word shows the variable assigned the other way earlier (by any thread)
-    bool bad = tn < 0;
+    bool bad = tn < 0 || (pre && d.tbad[t] != 0);
 #pragma unroll 4
-    for (int64_t i = tid; i < tn; i += NT) {
+    for (int64_t i = pre ? tn : tid; i < tn; i += NT) {
         const int32_t x = d.trail[tb + i];
         if (x == 0 || x > n || x < -n) {
             bad = true;
@@ -872,12 +873,14 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
         __syncthreads();   // the window's shared state is read before the next round rewrites it
     }
 
-    // ---- clear the assignment words this trail set (trail and implications)
-    for (int64_t i = tid; i < tn; i += NT) {
+    // ---- clear the assignment words this trail set (trail and implications);
+    // a trail's own words (apply_kernel) are cleared for the next launch by
+    // the host instead
+    for (int64_t i = pre ? tn : tid; i < tn; i += NT) {
         const int32_t x = d.trail[tb + i];
         if (x != 0 && x <= n && x >= -n) asg[((x > 0 ? x : -x) - 1) >> 4] = 0u;
     }
-    for (int64_t i = tid; i < n_impl; i += NT) asg[(impl[i] >> 1) >> 4] = 0u;
+    for (int64_t i = pre ? n_impl : tid; i < n_impl; i += NT) asg[(impl[i] >> 1) >> 4] = 0u;
 
     // ---- outputs
     myW = warp_sum(myW);

@@ -126,9 +126,9 @@ int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, const int64_t 
                          int32_t *impl_reason, int64_t *counters, void *stream);
 /* Host pointers: copies the trails in, runs, copies the results out, waits.
  * When every buffer is page-locked host memory (cudaHostAlloc, cudaHostRegister,
- * torch's pin_memory) the kernel reads the trails and writes the results in
- * place over the CPU-GPU link instead, with no staging copies; the results are
- * the same. */
+ * torch's pin_memory) the trails are copied in by DMA and the kernel writes the
+ * results in place over the CPU-GPU link, with no output staging; the results
+ * are the same. */
 int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets,
                        int32_t n_trails, int32_t *status, int32_t *conflict_clause,
                        int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,
@@ -141,7 +141,26 @@ int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
  * trails of very unequal length fewer trails in flight can finish sooner,
  * with equal ones all slots can (no counterpart in the reference). */
 int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n);
+/* The processing order of the runs that follow, when a run has more trails
+ * than it keeps in flight: trails whose literal count is nearest `pivot`
+ * start first (0, the default: shortest first).  A run lasts as long as its
+ * slowest trail; the slowest are those that reach their fixpoint without a
+ * conflict, which is likelier the fewer literals a trail assigns, but such a
+ * trail has fewer literals to propagate, so the slowest ones have a middling
+ * length that depends on the formula (BCPBatch.tune picks the pivot among
+ * quantiles of the caller's trail lengths).  Outputs do not depend on it.
+ * No counterpart in the reference, which propagates one trail at a time. */
+int gpsat_bcp_set_order_pivot(gpsat_bcp *b, int64_t pivot);
 
+/* Watch entries one round of the two-watched-literal kernel evaluates per
+ * trail (64, 128 or 256; default 128): one thread per entry, so the trail's
+ * thread block has entries / 32 warps.  Wider windows need fewer rounds per
+ * propagation but keep fewer trails in flight; outputs do not depend on it.
+ * (No counterpart in the reference, whose BCP is one thread per solver.) */
+int gpsat_bcp_set_window(gpsat_bcp *b, int32_t entries);
+/* Trails a window width keeps in flight at most: its resident blocks, within
+ * the workspace's slots. */
+int gpsat_bcp_window_slots(const gpsat_bcp *b, int32_t entries, int32_t *slots);
 /* The propagation strategy of the runs that follow (the reference chooses it at
  * compile time, SATSolver/Configs.cuh:27-33, CONFLICT_ANALYSIS_STRATEGY):
  *   GPSAT_BCP_WATCHED    two watched literals in the reference's order (default;
@@ -157,15 +176,6 @@ int gpsat_bcp_set_active_slots(gpsat_bcp *b, int32_t n);
  * Trails run one per thread block; a formula of up to 196,608 variables keeps a
  * trail's assignment in shared memory.  gpsat_bcp_run_static always runs
  * GPSAT_BCP_WATCHED. */
-/* Watch entries one round of the two-watched-literal kernel evaluates per
- * trail (64, 128 or 256; default 128): one thread per entry, so the trail's
- * thread block has entries / 32 warps.  Wider windows need fewer rounds per
- * propagation but keep fewer trails in flight; outputs do not depend on it.
- * (No counterpart in the reference, whose BCP is one thread per solver.) */
-int gpsat_bcp_set_window(gpsat_bcp *b, int32_t entries);
-/* Trails a window width keeps in flight at most: its resident blocks, within
- * the workspace's slots. */
-int gpsat_bcp_window_slots(const gpsat_bcp *b, int32_t entries, int32_t *slots);
 #define GPSAT_BCP_WATCHED 0
 #define GPSAT_BCP_FULL_SCAN 1
 int gpsat_bcp_set_strategy(gpsat_bcp *b, int32_t strategy);

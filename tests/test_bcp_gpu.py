@@ -239,6 +239,26 @@ def test_bcp_window_widths_agree(gpsat, orc, cuda_ok):
                counters=torch.empty(T, 6, dtype=torch.int64, device=dev))
     s = torch.cuda.Stream()
     times = b.tune(torch.from_numpy(tl).to(dev), torch.from_numpy(to).to(dev), out, s.cuda_stream)
-    assert b.window in (64, 128, 256) and (b.window, b.active) in times
+    assert b.window in (64, 128, 256) and (b.window, b.active, b.pivot) in times
     s.synchronize()
     compare_bcp({k: v.cpu().numpy() for k, v in out.items()}, o, label="after tuning")
+
+
+def test_bcp_order_pivot_does_not_change_outputs(gpsat, orc, cuda_ok):
+    """More trails than slots, so the processing order applies: trails nearest
+    each pivot first (0 = shortest first) give the same outputs as the oracle;
+    a negative pivot is refused."""
+    n = 5000
+    lits, off = gpsat.gen_random_ksat(46, n, 21000, 3)
+    tl, to = gpsat.gen_trails(47, n, 200, 0.005, 0.08)
+    b = gpsat.BCPBatch(gpsat.Formula(lits, off, n), impl_cap=2048)
+    b.set_active_slots(8)
+    o = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=2048, threads=8)
+    lens = np.diff(to)
+    for p in (0, int(np.median(lens)), int(lens.max()) + 1000, 1 << 40):
+        b.set_order_pivot(p)
+        g = b.run_host(tl, to)
+        compare_bcp(g, o, label=f"pivot {p}")
+        assert np.array_equal(g["counters"], o["counters"])
+    with pytest.raises(gpsat.GpsatError):
+        b.set_order_pivot(-1)
