@@ -189,14 +189,15 @@ def peaks():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def traffic_per_launch(n, trails, window, slots):
+def traffic_per_launch(n, trails, window, slots, pivot):
     """DRAM bytes of one launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)
     from the committed capture of this exact workload and launch shape, else None."""
     p = ROOT / "profiles" / "bcp_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    if (d.get("n_vars"), d.get("n_trails"), d.get("window"), d.get("slots")) != (n, trails, window, slots):
+    if (d.get("n_vars"), d.get("n_trails"), d.get("window"), d.get("slots"), d.get("order_pivot", 0)) != \
+            (n, trails, window, slots, pivot):
         return None
     return d["dram_bytes_per_launch"]
 
@@ -415,7 +416,7 @@ def run_gpu(args):
     avg_launch_s = elapsed / args.steps
     achieved = bytes_step / avg_launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic_per_launch(n, T, b.window, active), "peak_source": peak_src,
+            "traffic": traffic_per_launch(n, T, b.window, active, b.pivot), "peak_source": peak_src,
             "alg_bytes_per_launch": bytes_step, "kernel": f"gpsat::bcp::w{b.window // 32}::bcp_kernel"}
     cpu = None
     if not args.no_cpu:
