@@ -1350,6 +1350,7 @@ __device__ __forceinline__ void cdcl_body(const Params &P)
         if (lane == 0) job = (int)atomicAdd(P.next_job, 1u);
         job = __shfl_sync(FULL, job, 0);
         if (job >= P.n_jobs) break;
+        job = P.job_order[job];
         const int inst = P.job_inst[job];
         int64_t st[NSTATS];
         for (int i = 0; i < NSTATS; i++) st[i] = 0;

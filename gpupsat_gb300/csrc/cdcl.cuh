@@ -60,6 +60,7 @@ struct Params {
     const int64_t *var_off;      // per instance offset into per-var arrays (model, seeds, participation)
     // jobs
     const int32_t *job_inst, *job_cube_off, *job_cube_len, *cubes;
+    const int32_t *job_order;    // jobs in processing order (largest formula first)
     int32_t n_jobs;
     unsigned int *next_job;
     int32_t *inst_state;         // 0 open, 1 a job found a model

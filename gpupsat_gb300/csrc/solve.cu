@@ -97,6 +97,7 @@ struct gpsat_batch {
     int8_t *d_seed_phase = nullptr;
     // jobs
     int32_t *d_job_inst = nullptr, *d_job_cube_off = nullptr, *d_job_cube_len = nullptr, *d_cubes = nullptr;
+    int32_t *d_job_order = nullptr;
     int32_t *d_job_verdict = nullptr;
     int64_t *d_job_stats = nullptr;
     int64_t job_cap = 0, cube_cap = 0;
@@ -137,7 +138,7 @@ void batch_free(gpsat_batch *b)
                     b->d_oce, b->d_ocoff, b->d_model, b->d_state, b->d_verdict, b->d_ok, b->d_part,
                     b->d_seed_act, b->d_seed_phase, b->d_job_inst, b->d_job_cube_off, b->d_job_cube_len,
                     b->d_cubes, b->d_job_verdict, b->d_job_stats, b->d_counter, b->ws, b->d_proof,
-                    b->d_proof_len};
+                    b->d_proof_len, b->d_job_order};
     for (void *p : ptrs) cudaFree(p);
 }
 
@@ -450,11 +451,13 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         cudaFree(b->d_job_inst);
         cudaFree(b->d_job_cube_off);
         cudaFree(b->d_job_cube_len);
+        cudaFree(b->d_job_order);
         cudaFree(b->d_job_verdict);
         cudaFree(b->d_job_stats);
         b->job_cap = 0;
         if (!dalloc(&b->d_job_inst, J) || !dalloc(&b->d_job_cube_off, J) || !dalloc(&b->d_job_cube_len, J) ||
-            !dalloc(&b->d_job_verdict, J) || !dalloc(&b->d_job_stats, (size_t)J * cdcl::NSTATS))
+            !dalloc(&b->d_job_order, J) || !dalloc(&b->d_job_verdict, J) ||
+            !dalloc(&b->d_job_stats, (size_t)J * cdcl::NSTATS))
             return set_error(GPSAT_ERR_NOMEM, "job arrays");
         b->job_cap = J;
     }
@@ -498,10 +501,23 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         if (!dalloc(&b->d_part, PV)) return set_error(GPSAT_ERR_NOMEM, "part");
         b->part_cap = PV;
     }
+    // processing order: the jobs of the largest formulas first (the
+    // persistent grid takes them in this order).  A batch lasts as long as
+    // its slowest jobs, and at a fixed clause ratio the search grows with the
+    // variables, so the likely-long jobs should not start in the last wave.
+    // Each job's search and outputs do not depend on the order.
+    std::vector<int32_t> jorder(J);
+    for (int32_t j = 0; j < J; j++) jorder[j] = j;
+    std::stable_sort(jorder.begin(), jorder.end(), [&](int32_t a, int32_t c) {
+        const int32_t na = b->n_vars[jinst[a]], nc = b->n_vars[jinst[c]];
+        if (na != nc) return na > nc;
+        return b->prep[jinst[a]].n_clauses() > b->prep[jinst[c]].n_clauses();
+    });
     cudaStream_t st = 0;
     bool ok = true;
     if (J) {
         ok = cudaMemcpyAsync(b->d_job_inst, jinst.data(), J * 4, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+             cudaMemcpyAsync(b->d_job_order, jorder.data(), J * 4, cudaMemcpyHostToDevice, st) == cudaSuccess &&
              cudaMemcpyAsync(b->d_job_cube_off, jcoff.data(), J * 4, cudaMemcpyHostToDevice, st) == cudaSuccess &&
              cudaMemcpyAsync(b->d_job_cube_len, jclen.data(), J * 4, cudaMemcpyHostToDevice, st) == cudaSuccess;
         if (ok && !cubes.empty())
@@ -538,6 +554,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     P.job_inst = b->d_job_inst;
     P.job_cube_off = b->d_job_cube_off;
     P.job_cube_len = b->d_job_cube_len;
+    P.job_order = b->d_job_order;
     P.cubes = b->d_cubes;
     P.n_jobs = J;
     P.next_job = b->d_counter;
