@@ -90,6 +90,8 @@ def parse():
                          "seeding: learned VSIDS/phase seeding against plain solving")
     ap.add_argument("--n-range", type=int, nargs=2, default=[50, 250], help="solve: variables per instance")
     ap.add_argument("--conflict-budget", type=int, default=100000, help="solve/planted/seeding: per job")
+    ap.add_argument("--phase-init", type=int, default=0, choices=[0, 1, 2],
+                    help="planted: first polarity of a variable (0 false, 1 true, 2 its majority sign)")
     ap.add_argument("--train-instances", type=int, default=4096, help="seeding: training formulas")
     ap.add_argument("--epochs", type=int, default=3, help="seeding: training passes")
     ap.add_argument("--train-kind", default="random", choices=["random", "planted"], help="seeding: training set")
@@ -878,7 +880,7 @@ def run_planted_gpu(args):
     inst = planted_instances(args.instances)
     formulas = [(l, o) for _, l, o in inst]
     nv = [n for n, _, _ in inst]
-    opts = g.solve_options(conflict_budget=args.conflict_budget)
+    opts = g.solve_options(conflict_budget=args.conflict_budget, phase_init=args.phase_init)
     tuned = None
     if args.depth == "auto":
         depth, table = jobs.autotune_depth(formulas, nv, depths=(4, 6, 8, 10), sample=16, options=opts,
@@ -918,6 +920,7 @@ def run_planted_gpu(args):
             "data": "synthetic: seeded planted 3-SAT with 40 communities",
             "config": {"workload": "structured batch: planted community 3-SAT, n ~ U[2000,20000], m = 4.0 n",
                        "instances": args.instances, "cube_depth": depth, "depth_autotune": tuned,
+                       "phase_init": args.phase_init,
                        "jobs": int(len(jf)),
                        "chooser": "MaxClauseJobChooser ranking (reference VariableChooser score)",
                        "l2": "per-job state > L2; no flush needed"},

@@ -1130,6 +1130,20 @@ __device__ int solve_job(const Params &P, Ctx &C, int job, int inst, int64_t *st
     C.arena_top = C.orig_top = (int32_t)otop;
     C.n_crefs = C.n_orig = m;
     __syncwarp();
+    if (o.phase_init == 2 && !P.seed_phase) {
+        // first polarity = the sign the variable has in most of its clause
+        // occurrences (ties: false); lstamp counts, and is zero again after
+        for (uint32_t t = base + lane; t < P.coff[ce]; t += 32) {
+            const int32_t l = P.lits[t];
+            atomicAdd(&C.lstamp[l >> 1], (l & 1) ? 1 : -1);
+        }
+        __syncwarp();
+        for (int v = lane; v < C.n; v += 32) {
+            C.phase[v] = C.lstamp[v] > 0 ? 1 : 0;
+            C.lstamp[v] = 0;
+        }
+        __syncwarp();
+    }
     if (!rebuild_watches(C)) {
         stats[ST_FLAGS] |= FL_RESOURCE | ((int64_t)RS_INIT << 16);
         return R_UNKNOWN;

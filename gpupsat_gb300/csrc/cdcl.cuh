@@ -33,7 +33,7 @@ struct Opts {
     int32_t learnt_inc = 300;
     int32_t minimize = 1;
     int64_t conflict_budget = 100000;
-    int32_t phase_init = 0;          // 0: negative first, 1: positive first
+    int32_t phase_init = 0;          // 0: negative first, 1: positive first, 2: majority sign of the occurrences
     int32_t log_participation = 0;   // 1: participation counts; 2: and learnt-clause occurrences
     int32_t check_every = 256;       // conflicts between cancellation checks
 };

@@ -540,7 +540,8 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     P.o.learnt_inc = std::max(0, o.learnt_inc);
     P.o.minimize = o.minimize;
     P.o.conflict_budget = o.conflict_budget > 0 ? o.conflict_budget : INT64_MAX;
-    P.o.phase_init = o.phase_init ? 1 : 0;
+    if (o.phase_init < 0 || o.phase_init > 2) return set_error(GPSAT_ERR_ARG, "phase_init must be 0, 1 or 2");
+    P.o.phase_init = o.phase_init;
     P.o.log_participation = o.log_participation;
     P.o.check_every = 256;
     P.lits = b->d_lits;

@@ -230,7 +230,8 @@ typedef struct {
     int32_t learnt_inc;        /* growth of that limit per reduction */
     int32_t minimize;          /* ConflictAnalysis: basic learnt-clause minimisation */
     int64_t conflict_budget;   /* per job; reaching it ends the job UNKNOWN (0 = none) */
-    int32_t phase_init;        /* first polarity of an unseeded variable: 0 false, 1 true */
+    int32_t phase_init;        /* first polarity of an unseeded variable: 0 false, 1 true,
+                                  2 the sign of most of its occurrences in the formula */
     int32_t max_slots;         /* jobs in flight (0 = as many as the GPU keeps resident) */
     int32_t log_participation; /* 1: count, per variable, the conflicts whose analysis saw it;
                                   2: also its occurrences in learnt clauses */

@@ -45,11 +45,12 @@ def random_n50(gpsat, solve_golden):
     return rs, [gpsat.gen_random_ksat(r["seed"], r["n"], r["m"], 3) for r in rs], [r["n"] for r in rs]
 
 
-@pytest.mark.parametrize("mode", ["vsids_luby", "vsids_geometric", "last_free", "no_minimize"])
+@pytest.mark.parametrize("mode", ["vsids_luby", "vsids_geometric", "last_free", "no_minimize", "majority_phase"])
 def test_random_n50_matches_reference(gpsat, cuda_ok, solve_golden, mode):
     rs, formulas, nv = random_n50(gpsat, solve_golden)
     opts = dict(vsids_luby={}, vsids_geometric=dict(restart=gpsat.RESTART_GEOMETRIC, restart_factor=1.3),
-                last_free=dict(decide=gpsat.DECIDE_LAST_FREE), no_minimize=dict(minimize=0))[mode]
+                last_free=dict(decide=gpsat.DECIDE_LAST_FREE), no_minimize=dict(minimize=0),
+                majority_phase=dict(phase_init=2))[mode]
     out = solve_all(gpsat, formulas, nv, **opts)
     ref = [r["ref_nocap"] for r in rs]
     assert list(out["verdict"]) == ref
