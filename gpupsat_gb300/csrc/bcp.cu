@@ -106,14 +106,15 @@ constexpr int APPLY_NT = 512;
 constexpr int APPLY_CHUNK_WORDS = 16384;   // 64 KB: 262,144 variables per pass
 constexpr int64_t APPLY_MAX_BYTES = int64_t(8) << 30;   // above this the blocks assign their own trails
 
+// trails [t_begin, t_end) of the launch
 __global__ void __launch_bounds__(APPLY_NT) apply_kernel(const int32_t *__restrict__ trail,
-                                                        const int64_t *__restrict__ toff, int32_t n_trails,
-                                                        int32_t n, int64_t n_words, uint32_t *__restrict__ tasg,
-                                                        int32_t *__restrict__ tbad)
+                                                        const int64_t *__restrict__ toff, int32_t t_begin,
+                                                        int32_t t_end, int32_t n, int64_t n_words,
+                                                        uint32_t *__restrict__ tasg, int32_t *__restrict__ tbad)
 {
     extern __shared__ uint32_t chunk[];   // APPLY_CHUNK_WORDS words
     __shared__ int s_bad;
-    for (int t = blockIdx.x; t < n_trails; t += gridDim.x) {
+    for (int t = t_begin + blockIdx.x; t < t_end; t += gridDim.x) {
         const int64_t tb = toff[t], tn = toff[t + 1] - tb;
         uint32_t *out = tasg + (size_t)t * n_words;
         if (threadIdx.x == 0) s_bad = tn < 0;
@@ -414,6 +415,10 @@ struct gpsat_bcp {
     int32_t *tbad = nullptr;
     int64_t tasg_cap = 0, tbad_cap = 0;   // words, trails
     int32_t apply_blocks = 0;             // resident blocks of apply_kernel (0: not looked up yet)
+    // page-locked host trails: copied in parts on copy_stream, each part
+    // applied on the launch stream as soon as it has arrived
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t part_done[4] = {};
 };
 
 namespace {
@@ -435,12 +440,17 @@ void bcp_free(gpsat_bcp *b)
     cudaFree(b->d_out);
     cudaFree(b->tasg);
     cudaFree(b->tbad);
+    for (cudaEvent_t e : b->part_done)
+        if (e) cudaEventDestroy(e);
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
 }
 
 // Trail t's assignment words built ahead of the BCP kernel into tasg (grown
 // on demand); false when they would take more than APPLY_MAX_BYTES or cannot
 // be allocated, and the BCP kernel's blocks then assign their own trails.
-bool apply_trails(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, cudaStream_t st)
+// The per-trail words and flags for n_trails trails; false when they would
+// take more than APPLY_MAX_BYTES or cannot be allocated.
+bool apply_prepare(gpsat_bcp *b, int32_t n_trails)
 {
     const int64_t words = (int64_t)n_trails * b->n_words;
     if (n_trails <= 0 || words * 4 > bcp::APPLY_MAX_BYTES) return false;
@@ -478,15 +488,28 @@ bool apply_trails(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32
             cudaGetLastError();
         b->apply_blocks = std::max(1, sms * std::max(per_sm, 1));
     }
-    const int grid = std::min<int32_t>(n_trails, b->apply_blocks);
-    bcp::apply_kernel<<<grid, bcp::APPLY_NT, bcp::APPLY_CHUNK_WORDS * 4, st>>>(trail, toff, n_trails, b->f->h.n_vars,
+    return true;
+}
+
+// apply_kernel over trails [t0, t1) on stream st (after apply_prepare)
+bool apply_range(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t t0, int32_t t1, cudaStream_t st)
+{
+    if (t1 <= t0) return true;
+    const int grid = std::min<int32_t>(t1 - t0, b->apply_blocks);
+    bcp::apply_kernel<<<grid, bcp::APPLY_NT, bcp::APPLY_CHUNK_WORDS * 4, st>>>(trail, toff, t0, t1, b->f->h.n_vars,
                                                                                b->n_words, b->tasg, b->tbad);
     return cudaGetLastError() == cudaSuccess;
 }
 
+bool apply_trails(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, cudaStream_t st)
+{
+    return apply_prepare(b, n_trails) && apply_range(b, trail, toff, 0, n_trails, st);
+}
+
+// applied: the caller already ran apply_kernel over every trail into b->tasg
 int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_trails, int32_t *status,
            int32_t *conflict, int32_t *stop, int64_t *nimpl, int32_t *ilit, int32_t *ireason, int64_t *counters,
-           cudaStream_t st)
+           cudaStream_t st, bool applied = false)
 {
     const gpsat_formula *f = b->f;
     bcp::Dev d{};
@@ -558,7 +581,7 @@ int launch(gpsat_bcp *b, const int32_t *trail, const int64_t *toff, int32_t n_tr
             bcp::scan_kernel<false><<<d.n_slots, bcp::SCAN_NT, 0, st>>>(d, f->d_coff);
         err = cudaGetLastError();
     } else {
-        if (apply_trails(b, trail, toff, n_trails, st)) {
+        if (applied || apply_trails(b, trail, toff, n_trails, st)) {
             d.tasg = b->tasg;
             d.tbad = b->tbad;
         }
@@ -718,12 +741,9 @@ extern "C" int gpsat_bcp_run_device(gpsat_bcp *b, const int32_t *trail_lits, con
 }
 
 namespace {
-// The trails copied into the handle's staging buffers (grown on demand) on
-// stream st: device memory that apply_kernel can pass over more than once.
-int stage_trails(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails,
-                 cudaStream_t st)
+// The handle's trail staging buffers, grown to nl literals and n_trails trails.
+int stage_alloc(gpsat_bcp *b, int64_t nl, int32_t n_trails)
 {
-    const int64_t nl = trail_offsets[n_trails];
     if (nl > b->trail_cap) {
         cudaFree(b->d_trail);
         b->d_trail = nullptr;
@@ -742,12 +762,66 @@ int stage_trails(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_o
         }
         b->toff_cap = n_trails + 1;
     }
+    return GPSAT_OK;
+}
+
+// The trails copied into the handle's staging buffers (grown on demand) on
+// stream st: device memory that apply_kernel can pass over more than once.
+int stage_trails(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails,
+                 cudaStream_t st)
+{
+    const int64_t nl = trail_offsets[n_trails];
+    const int rc = stage_alloc(b, nl, n_trails);
+    if (rc != GPSAT_OK) return rc;
     if (nl > 0 && cudaMemcpyAsync(b->d_trail, trail_lits, nl * 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return cuda_error(cudaGetLastError(), "trail copy");
     if (cudaMemcpyAsync(b->d_toff, trail_offsets, (int64_t)(n_trails + 1) * 8, cudaMemcpyHostToDevice, st) !=
         cudaSuccess)
         return cuda_error(cudaGetLastError(), "offset copy");
     return GPSAT_OK;
+}
+// Page-locked host trails: copied to the staging buffers in parts on the
+// handle's copy stream, each part's trails applied (apply_kernel) on the
+// legacy stream as soon as the part has arrived, so the copy of one part
+// overlaps the application of the one before.  False (nothing enqueued that
+// matters: the caller copies and applies as usual) when a stream, an event or
+// the per-trail words cannot be had.
+bool copy_and_apply(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trail_offsets, int32_t n_trails)
+{
+    constexpr int P = 4;
+    if (!apply_prepare(b, n_trails)) return false;
+    if (!b->copy_stream) {
+        if (cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            b->copy_stream = nullptr;
+            return false;
+        }
+        for (cudaEvent_t &e : b->part_done)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                e = nullptr;
+            }
+    }
+    for (cudaEvent_t e : b->part_done)
+        if (!e) return false;
+    cudaStream_t cs = b->copy_stream;
+    // the legacy stream's earlier work (a previous run's readers of the
+    // staging buffers) is done before the copies start: run_host synchronises
+    if (cudaMemcpyAsync(b->d_toff, trail_offsets, (int64_t)(n_trails + 1) * 8, cudaMemcpyHostToDevice, cs) !=
+        cudaSuccess)
+        return cudaGetLastError(), false;
+    for (int k = 0; k < P; k++) {
+        const int32_t t0 = (int32_t)((int64_t)n_trails * k / P), t1 = (int32_t)((int64_t)n_trails * (k + 1) / P);
+        const int64_t a = trail_offsets[t0], e = trail_offsets[t1];
+        if (e > a && cudaMemcpyAsync(b->d_trail + a, trail_lits + a, (e - a) * 4, cudaMemcpyHostToDevice, cs) !=
+                         cudaSuccess)
+            return cudaGetLastError(), false;
+        if (cudaEventRecord(b->part_done[k], cs) != cudaSuccess || cudaStreamWaitEvent(0, b->part_done[k], 0) !=
+                                                                          cudaSuccess)
+            return cudaGetLastError(), false;
+        if (!apply_range(b, b->d_trail, b->d_toff, t0, t1, 0)) return false;
+    }
+    return true;
 }
 }  // namespace
 
@@ -784,10 +858,16 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
             }
         }
         if (all) {
-            int rc = stage_trails(b, trail_lits, trail_offsets, n_trails, 0);
+            int rc = stage_alloc(b, nl, n_trails);
             if (rc != GPSAT_OK) return rc;
+            const bool applied = b->strategy == GPSAT_BCP_WATCHED && copy_and_apply(b, trail_lits, trail_offsets, n_trails);
+            if (!applied) {
+                rc = stage_trails(b, trail_lits, trail_offsets, n_trails, 0);
+                if (rc != GPSAT_OK) return rc;
+            }
             rc = launch(b, b->d_trail, b->d_toff, n_trails, (int32_t *)dp[2], (int32_t *)dp[3], (int32_t *)dp[4],
-                        (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7], counters ? (int64_t *)dp[8] : nullptr, 0);
+                        (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7], counters ? (int64_t *)dp[8] : nullptr, 0,
+                        applied);
             if (rc != GPSAT_OK) return rc;
             err = cudaStreamSynchronize(0);
             if (err != cudaSuccess) return cuda_error(err, "bcp run");
