@@ -102,7 +102,7 @@ struct Smem {
     int32_t mh[2 * W];         // move targets of the round (collision check)
     int collide;
     int32_t mv_t1[W], mv_t2[W];
-    int32_t confl_c, confl_scan;
+    int32_t confl_c[2], confl_scan[2];   // by round parity (see the round's end)
     unsigned long long red[NW][3];
     int t;
     // look-ahead ring: trail position q lives in slot q % LB
@@ -225,6 +225,7 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
     // every iteration finishes a scan, pops a frame or commits at least one
     // entry; the budget only guarantees termination if that were ever broken
     int64_t budget = MAX_ITERS;
+    int par = 0;   // round parity: the slot of this round's conflict record
 
     while (status == GPSAT_BCP_NO_CONFLICT) {
         if (--budget < 0) {
@@ -307,7 +308,7 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             sm.key_min = NO_CUT;
             sm.imp_cnt = 0;
             sm.collide = 0;
-            sm.confl_c = -1;
+            sm.confl_c[par] = -1;
         }
         int ndyn = 0;
         bool dyn_done = true;
@@ -658,7 +659,9 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             }
             my_im = bim + __popc(bi & lt);
             my_mv = bmv + __popc(b1 & lt) + __popc(b2 & lt);
-            __syncthreads();   // the counts are read before anyone writes them again
+            // (no barrier here: the counts are written again only after the
+            // commit barrier of this round, or after the barrier that
+            // precedes the second call below)
         };
         rank();
         // more implications than impl_cap leaves room for: commit up to the
@@ -773,8 +776,8 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             atomicOr(&asg[u >> 4], ((r.unit & 1) ? 3u : 1u) << ((u & 15) << 1));
         }
         if (com && r.act == A_CONFLICT) {
-            sm.confl_c = en.x;
-            sm.confl_scan = my_scan;
+            sm.confl_c[par] = en.x;
+            sm.confl_scan[par] = my_scan;
         }
         if (com) {
             myW++;
@@ -815,15 +818,17 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             }
         }
         if (refill) ring_hi = ring_hi + CHUNK < tn ? ring_hi + CHUNK : tn;
-        __syncthreads();
-        // empty the move-target table for the next round (the end-of-round
-        // barrier separates this from the next round's inserts)
+        // empty the move-target table for the next round (every probe of
+        // this round came before the collision barrier; the next round's
+        // inserts come after this round's last barrier)
         for (int i = tid; i < 2 * W; i += NT) sm.mh[i] = -1;
         arena_used += tot_mv;
         n_impl += tot_im;
         cI += tot_im;
 
-        // ---- advance the scan cursors
+        // ---- advance the scan cursors (from window state that no thread
+        // writes before the next round's layout)
+        bool reload = false;
         if (new_cur == 0) {
             if (k_end > 0) {
                 if (k_end <= ndyn) {
@@ -841,9 +846,9 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             cur_dp = -1;
             if (!new_started) {
                 // cut before this scan because its list is not what the window
-                // assumed (possibly changed by this round): read it again
-                const uint32_t h = dh[cur_var];
-                cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+                // assumed (possibly changed by this round): read it again once
+                // this round's list-head writes are in
+                reload = true;
             } else {
                 const int k = k_end - sm.sc_b[new_cur];
                 if (sm.sc_head[new_cur] >= 0) {
@@ -863,14 +868,25 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             depth = 0;  // a descent whose scan led into trail scans has ended
             cur_impl_start = n_impl - tot_im;
         }
-        const int32_t cc = sm.confl_c;
+        // The round's one closing barrier: this round's commits (list heads,
+        // clause states, ring, conflict record) are in before anyone reads
+        // them, and every read of this round's window state is done before
+        // the next layout rewrites it.  The conflict record alternates
+        // between two slots, so the next layout's reset of its own slot cannot
+        // race with a late read of this one.
+        __syncthreads();
+        if (reload) {
+            const uint32_t h = dh[cur_var];
+            cur_dp = ((h >> 24) == e) ? (int32_t)(h & 0xFFFFFFu) : -1;
+        }
+        const int32_t cc = sm.confl_c[par];
         if (cc >= 0) {
-            const int ks = sm.confl_scan;
+            const int ks = sm.confl_scan[par];
             confl = cc;
             stopi = (int32_t)(ks == 0 ? (new_cur == 0 ? cur_trail : dfs_trail) : ti_round + ks - 1);
             status = GPSAT_BCP_CONFLICT;
         }
-        __syncthreads();   // the window's shared state is read before the next round rewrites it
+        par ^= 1;
     }
 
     // ---- clear the assignment words this trail set (trail and implications);
