@@ -663,6 +663,33 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             // commit barrier of this round, or after the barrier that
             // precedes the second call below)
         };
+        // the round's moves into the move-target table before the ranking
+        // barrier, which publishes both.  Moves into the same variable within
+        // the round (rare) are linked by thread 0 in window order; otherwise
+        // every mover links its own entry.  (If the implication limit below
+        // shortens the commit, the entries it drops may leave false
+        // collisions: they only send the round to the serial path.)
+        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
+            const int32_t tg[2] = {r.t1, r.t2};
+            for (int k = 0; k < (r.act == A_SW2 ? 2 : 1); k++) {
+                const uint32_t hsh = ((uint32_t)tg[k] * 2654435761u) >> 24;
+                for (int probe = 0; probe < 2 * W; probe++) {
+                    const int slotp = (int)((hsh + (uint32_t)probe) & (2 * W - 1));
+                    const int32_t old = atomicCAS(&sm.mh[slotp], -1, tg[k]);
+                    if (old == -1) break;
+                    if (old == tg[k]) {
+                        sm.collide = 1;
+                        break;
+                    }
+                }
+            }
+        }
+        sm.mv_t1[tid] = (com && (r.act == A_SW1 || r.act == A_SW2)) ? r.t1 : -1;
+        sm.mv_t2[tid] = (com && r.act == A_SW2) ? r.t2 : -1;
+        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
+            sm.dyn0[tid] = make_int4(en.x, en.y, en.z, 0);
+            sm.dyn1[tid] = el;
+        }
         rank();
         // more implications than impl_cap leaves room for: commit up to the
         // first one that does not fit; the next round reports the overflow there
@@ -691,36 +718,15 @@ __device__ void process_trail(const Dev &d, Smem &sm, const int t, const int slo
             if (first) sm.nsc = my_scan;
             __syncthreads();
             const int ks = sm.nsc;
+            for (int i = tid; i < 2 * W; i += NT) sm.mh[i] = -1;   // clean for the next trail
             status = GPSAT_BCP_OVERFLOW;
             stopi = (int32_t)(ks == 0 ? cur_trail : ti + ks - 1);
             break;
         }
 
         // ---- commit
-        // moves into the same variable within the round (rare) are linked by
-        // thread 0 in window order; otherwise every mover links its own entry
-        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
-            const int32_t tg[2] = {r.t1, r.t2};
-            for (int k = 0; k < (r.act == A_SW2 ? 2 : 1); k++) {
-                const uint32_t hsh = ((uint32_t)tg[k] * 2654435761u) >> 24;
-                for (int probe = 0; probe < 2 * W; probe++) {
-                    const int slotp = (int)((hsh + (uint32_t)probe) & (2 * W - 1));
-                    const int32_t old = atomicCAS(&sm.mh[slotp], -1, tg[k]);
-                    if (old == -1) break;
-                    if (old == tg[k]) {
-                        sm.collide = 1;
-                        break;
-                    }
-                }
-            }
-        }
-        sm.mv_t1[tid] = (com && (r.act == A_SW1 || r.act == A_SW2)) ? r.t1 : -1;
-        sm.mv_t2[tid] = (com && r.act == A_SW2) ? r.t2 : -1;
-        if (com && (r.act == A_SW1 || r.act == A_SW2)) {
-            sm.dyn0[tid] = make_int4(en.x, en.y, en.z, 0);
-            sm.dyn1[tid] = el;
-        }
-        __syncthreads();
+        // (the move-target table and the movers' records were published by
+        // the ranking barrier)
         const bool collide = sm.collide != 0;
         if (!collide) {
             if (com && (r.act == A_SW1 || r.act == A_SW2)) {
