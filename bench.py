@@ -105,6 +105,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=60.0, help="reference solve sample: wall budget")
     ap.add_argument("--ref-budget", type=float, default=5.0,
                     help="reference solve sample: wall seconds per instance before it counts as ref-undecided")
+    ap.add_argument("--ref-own-trails", type=int, default=1024,
+                    help="reference arm: trails of the reference's own BCP timed at n=2000")
     ap.add_argument("--no-solve", action="store_true", help="bcp: leave out the batched-solve measurement")
     ap.add_argument("--no-latency", action="store_true", help="bcp: leave out the single-instance measurement")
     ap.add_argument("--solve-instances", type=int, default=16384, help="bcp: instances of the solve measurement")
@@ -254,7 +256,7 @@ def run_reference(args):
                                        f"BCP cannot hold n=1e6 (100k-node watch pool, O(n) per assignment), so "
                                        f"its C restatement (oracle/bcp_ref.c, bit-exact with it) is timed"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    line["cpu_baseline"]["ref_own_scaled"] = ref_own_bcp_scaled()
+    line["cpu_baseline"]["ref_own_scaled"] = ref_own_bcp_scaled(trails=args.ref_own_trails)
     if not args.no_solve:
         line["solve"] = solve_object_ref(args)
     if not args.no_latency:
