@@ -679,7 +679,10 @@ extern "C" int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *devic
 {
     if (!b) return set_error(GPSAT_ERR_ARG, "null handle");
     if (slots) *slots = b->slots;
-    if (device_bytes) *device_bytes = b->bytes;
+    // the slots, plus the per-trail assignment words and staging buffers the
+    // runs so far have grown
+    if (device_bytes)
+        *device_bytes = b->bytes + b->tasg_cap * 4 + b->tbad_cap * 4 + b->trail_cap * 4 + b->toff_cap * 8 + b->out_cap;
     return GPSAT_OK;
 }
 

@@ -133,7 +133,8 @@ int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *t
                        int32_t n_trails, int32_t *status, int32_t *conflict_clause,
                        int32_t *stop_index, int64_t *n_impl, int32_t *impl_lit,
                        int32_t *impl_reason, int64_t *counters);
-/* Trails in flight and the device bytes the workspace holds. */
+/* Trails in flight and the device bytes the workspace holds (its slots, and
+ * the per-trail assignment words and staging buffers earlier runs grew). */
 int gpsat_bcp_info(const gpsat_bcp *b, int32_t *slots, int64_t *device_bytes);
 /* Runs that follow use at most n of the workspace's slots (1 <= n <= slots;
  * 0 = all).  Outputs do not depend on it.  A launch lasts as long as its
