@@ -122,6 +122,20 @@ public:
     TrailPropagator(const TrailPropagator &) = delete;
     TrailPropagator &operator=(const TrailPropagator &) = delete;
 
+    // The reference's CONFLICT_ANALYSIS_STRATEGY (SATSolver/Configs.cuh:27-33):
+    // two watched literals (default) or full-scan clause evaluation
+    // (BASIC_SEARCH, ConflictAnalysis/ConflictAnalyzer.cu:173-245).
+    void use_full_scan(bool on)
+    {
+        check(gpsat_bcp_set_strategy(h_, on ? GPSAT_BCP_FULL_SCAN : GPSAT_BCP_WATCHED), "bcp strategy");
+    }
+    // Launch shape of the two-watched-literal kernel (outputs do not depend
+    // on it): watch entries per round (64, 128, 256), trails in flight (0:
+    // all resident), and the processing order's length pivot (0: shortest first).
+    void set_window(int32_t entries) { check(gpsat_bcp_set_window(h_, entries), "bcp window"); }
+    void set_active_slots(int32_t n) { check(gpsat_bcp_set_active_slots(h_, n), "bcp slots"); }
+    void set_order_pivot(int64_t pivot) { check(gpsat_bcp_set_order_pivot(h_, pivot), "bcp order pivot"); }
+
     std::vector<TrailOutcome> new_decisions(const std::vector<std::vector<int32_t>> &trails)
     {
         const int32_t T = (int32_t)trails.size();

@@ -1,10 +1,15 @@
 // Exercises the C++ host interface (include/gpsat.hpp) from a program that
 // includes it, as a user of the library would.
 //   api_check rank  <cnf> <depth>       chosen split variables of MaxClauseJobChooser
-//   api_check trails <cnf> <trail file> TrailPropagator over the trails (one per
+//   api_check trails <cnf> <trail file> [scan]
+//                                       TrailPropagator over the trails (one per
 //                                        line, DIMACS literals ending in 0): one
 //                                        line per trail: status conflict stop
-//                                        n_implied then (literal reason) pairs
+//                                        n_implied then (literal reason) pairs;
+//                                        "scan": the full-scan strategy, with a
+//                                        256-entry window and 8 trails in flight
+//                                        set on the way (the watched kernel's
+//                                        shape, which the full scan ignores)
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -44,6 +49,12 @@ int main(int argc, char **argv)
             }
             gpsat::Formula fo(f);
             gpsat::TrailPropagator bcp(fo, 4096);
+            if (argc > 4 && std::string(argv[4]) == "scan") {
+                bcp.set_window(256);
+                bcp.set_active_slots(8);
+                bcp.set_order_pivot(100);
+                bcp.use_full_scan(true);
+            }
             for (const gpsat::TrailOutcome &o : bcp.new_decisions(trails)) {
                 std::printf("%d %d %d %zu", o.status, o.conflict_clause, o.stop_index, o.implied.size());
                 for (size_t i = 0; i < o.implied.size(); i++) std::printf(" %d %d", o.implied[i], o.reasons[i]);

@@ -99,7 +99,8 @@ def test_device_entries_reject_a_null_trail(gpsat):
 
 
 @pytest.mark.gpu
-def test_trail_propagator_matches_the_oracle(gpsat, orc, api_check, cuda_ok, tmp_path):
+@pytest.mark.parametrize("strategy", ["watched", "full_scan"])
+def test_trail_propagator_matches_the_oracle(gpsat, orc, api_check, cuda_ok, tmp_path, strategy):
     n, m, T = 3000, 12600, 24
     lits, off = gpsat.gen_random_ksat(31, n, m, 3)
     tl, to = gpsat.gen_trails(32, n, T, 0.01, 0.12)
@@ -107,9 +108,10 @@ def test_trail_propagator_matches_the_oracle(gpsat, orc, api_check, cuda_ok, tmp
     write_cnf(cnf, lits, off, n)
     tr = tmp_path / "trails.txt"
     tr.write_text("".join(" ".join(str(int(x)) for x in tl[to[t]:to[t + 1]]) + " 0\n" for t in range(T)))
-    r = subprocess.run([str(api_check), "trails", str(cnf), str(tr)], capture_output=True, text=True)
+    extra = ["scan"] if strategy == "full_scan" else []
+    r = subprocess.run([str(api_check), "trails", str(cnf), str(tr), *extra], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    ref = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=4096)
+    ref = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=4096, strategy=strategy)
     rows = r.stdout.strip().split("\n")
     assert len(rows) == T
     for t, row in enumerate(rows):
