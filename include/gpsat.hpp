@@ -222,7 +222,7 @@ struct ClauseLearning {
 // keeps learnt clauses, halving the worst by LBD when the limit is reached
 struct LearntClauseDatabase : ClauseLearning {
     int32_t first, inc;
-    LearntClauseDatabase(int32_t f = 2000, int32_t i = 300) : first(f), inc(i) {}
+    LearntClauseDatabase(int32_t f = 6000, int32_t i = 300) : first(f), inc(i) {}
     void configure(gpsat_solve_options &o) const override
     {
         o.learnt_first = first;
