@@ -618,7 +618,7 @@ def solve_config(args, instances=None):
     lo, hi = args.n_range
     return {"workload": f"batched solve: random 3-SAT, n ~ U[{lo},{hi}], m = round(4.26 n)",
             "instances": instances or args.instances, "conflict_budget": args.conflict_budget,
-            "decisions": "VSIDS", "restarts": "Luby 100",
+            "decisions": "VSIDS", "restarts": "Luby 400", "vsids_decay": 0.99, "clause_db": "6000 + 300",
             "l2": "per-job state > L2 (one workspace slot per resident warp); no flush needed"}
 
 

@@ -188,7 +188,7 @@ struct DecisionStrategy {
 };
 struct VSIDS : DecisionStrategy {
     float decay;
-    explicit VSIDS(float d = 0.95f) : decay(d) {}
+    explicit VSIDS(float d = 0.99f) : decay(d) {}
     void configure(gpsat_solve_options &o) const override
     {
         o.decide = GPSAT_DECIDE_VSIDS;
@@ -250,7 +250,7 @@ struct GeometricRestarts : Restarts {  // reference defaults: 100 conflicts, x1.
 };
 struct LubyRestarts : Restarts {
     int32_t unit;
-    explicit LubyRestarts(int32_t u = 100) : unit(u) {}
+    explicit LubyRestarts(int32_t u = 400) : unit(u) {}
     void configure(gpsat_solve_options &o) const override
     {
         o.restart = GPSAT_RESTART_LUBY;

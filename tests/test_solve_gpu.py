@@ -48,7 +48,7 @@ def random_n50(gpsat, solve_golden):
 @pytest.mark.parametrize("mode", ["vsids_luby", "vsids_geometric", "last_free", "no_minimize", "majority_phase"])
 def test_random_n50_matches_reference(gpsat, cuda_ok, solve_golden, mode):
     rs, formulas, nv = random_n50(gpsat, solve_golden)
-    opts = dict(vsids_luby={}, vsids_geometric=dict(restart=gpsat.RESTART_GEOMETRIC, restart_factor=1.3),
+    opts = dict(vsids_luby={}, vsids_geometric=dict(restart=gpsat.RESTART_GEOMETRIC, restart_base=100, restart_factor=1.3),
                 last_free=dict(decide=gpsat.DECIDE_LAST_FREE), no_minimize=dict(minimize=0),
                 majority_phase=dict(phase_init=2))[mode]
     out = solve_all(gpsat, formulas, nv, **opts)
