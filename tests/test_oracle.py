@@ -2,6 +2,7 @@
 preprocessing are pinned to golden vectors produced by the reference itself
 (tests/golden/make_golden.py)."""
 import numpy as np
+import pytest
 
 from conftest import compare_bcp
 
@@ -73,3 +74,61 @@ def test_oracle_full_scan_matches_reference_golden(orc, scan_golden):
                 f"case {ci} trail {t}"
             assert np.array_equal(r["impl_lit"][t, :k], c["impl_lit"][t, :k]), f"case {ci} trail {t}: implied literals"
         assert (c["status"] == 1).any() and (c["status"] == 0).any()
+
+
+def _check_outputs(cl, n, tl, to, r, strategy):
+    """The properties the reference's own unit tests assert of its BCP
+    (UnitTesting: every implication has a clause that is unit for it; a
+    conflict clause is all false), on the oracle's outputs."""
+    BIG = np.int64(1) << 40
+    for t in range(len(to) - 1):
+        tr = tl[to[t]:to[t + 1]]
+        k = int(r["n_impl"][t])
+        imp = r["impl_lit"][t, :k]
+        sgn = np.zeros(n + 1, np.int8)
+        pos = np.full(n + 1, BIG, np.int64)
+        sgn[np.abs(tr)] = np.sign(tr)
+        pos[np.abs(tr)] = -1
+        assert (pos[np.abs(imp)] == BIG).all(), f"{strategy} trail {t}: implied an assigned variable"
+        sgn[np.abs(imp)] = np.sign(imp)
+        pos[np.abs(imp)] = np.arange(k)
+        if k:
+            rc = cl[r["impl_reason"][t, :k]]
+            is_unit = rc == imp[:, None]
+            assert is_unit.sum(1).min() == 1
+            false_before = (sgn[np.abs(rc)] == -np.sign(rc)) & (pos[np.abs(rc)] < np.arange(k)[:, None])
+            assert (false_before | is_unit).all(), f"{strategy} trail {t}: a reason clause is not unit"
+        if r["status"][t] == 1:
+            c = cl[r["conflict"][t]]
+            assert (sgn[np.abs(c)] == -np.sign(c)).all(), f"{strategy} trail {t}: conflict clause not false"
+
+
+@pytest.mark.parametrize("strategy", ["watched", "full_scan"])
+def test_oracle_outputs_keep_the_reference_invariants(gpsat, orc, strategy):
+    n, m, T = 3000, 12600, 128
+    lits, off = gpsat.gen_random_ksat(77, n, m, 3)
+    tl, to = gpsat.gen_trails(78, n, T, 0.01, 0.08)
+    r = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=n, threads=4, strategy=strategy)
+    assert set(np.unique(r["status"])) <= {0, 1} and (r["status"] == 1).any() and (r["status"] == 0).any()
+    _check_outputs(lits.reshape(-1, 3), n, tl, to, r, strategy)
+
+
+def test_oracle_implies_the_last_literal_of_a_falsified_clause(gpsat, orc):
+    """The reference's WatchedClausesList test: falsify all but the last
+    literal of a clause and the last one is implied (or the trail conflicts
+    before the propagation reaches it)."""
+    n, m = 2000, 8400
+    lits, off = gpsat.gen_random_ksat(79, n, m, 3)
+    cl = lits.reshape(-1, 3)
+    rng = np.random.default_rng(80)
+    picks = rng.choice(m, 64, replace=False)
+    trails = [(-cl[c, :2]).astype(np.int32) for c in picks]
+    to = np.zeros(len(trails) + 1, np.int64)
+    to[1:] = np.cumsum([len(t) for t in trails])
+    tl = np.concatenate(trails)
+    r = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=n, threads=4)
+    for j, c in enumerate(picks):
+        if r["status"][j] == 1:
+            continue
+        k = int(r["n_impl"][j])
+        assert cl[c, 2] in r["impl_lit"][j, :k], f"clause {c}: its last literal was not implied"
