@@ -284,7 +284,17 @@ def ref_own_bcp_scaled(n=2000, trails=1024):
     trail application alone (the driver times the assignments and the
     new_decision calls, not the watch-list set-up before them)."""
     import oracle
-    L = _ref_lib("stock")
+    try:
+        L = _ref_lib("stock")
+    except OSError:
+        # not built yet here: build it from the reference sources or the
+        # carried build-dir copy, else report why there is no figure
+        try:
+            from oracle.ref import build_ref
+            build_ref.build()
+            L = _ref_lib("stock")
+        except (OSError, FileNotFoundError, subprocess.CalledProcessError) as e:
+            return {"unavailable": f"the reference's host build is not available here: {e}"}
     m = int(round(4.2 * n))
     lits, off = oracle.gen_random_ksat(2024, n, m, 3)
     tl, to = oracle.gen_trails(7, n, trails, 0.01, 0.05)
