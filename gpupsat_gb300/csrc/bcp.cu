@@ -445,11 +445,10 @@ void bcp_free(gpsat_bcp *b)
     if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
 }
 
-// Trail t's assignment words built ahead of the BCP kernel into tasg (grown
-// on demand); false when they would take more than APPLY_MAX_BYTES or cannot
-// be allocated, and the BCP kernel's blocks then assign their own trails.
-// The per-trail words and flags for n_trails trails; false when they would
-// take more than APPLY_MAX_BYTES or cannot be allocated.
+// Room for n_trails trails' assignment words (tasg) and bad-trail flags
+// (tbad), built by apply_kernel ahead of the BCP kernel and grown on demand;
+// false when they would take more than APPLY_MAX_BYTES or cannot be
+// allocated, and the BCP kernel's blocks then assign their own trails.
 bool apply_prepare(gpsat_bcp *b, int32_t n_trails)
 {
     const int64_t words = (int64_t)n_trails * b->n_words;
@@ -810,21 +809,26 @@ bool copy_and_apply(gpsat_bcp *b, const int32_t *trail_lits, const int64_t *trai
     cudaStream_t cs = b->copy_stream;
     // the legacy stream's earlier work (a previous run's readers of the
     // staging buffers) is done before the copies start: run_host synchronises
-    if (cudaMemcpyAsync(b->d_toff, trail_offsets, (int64_t)(n_trails + 1) * 8, cudaMemcpyHostToDevice, cs) !=
-        cudaSuccess)
-        return cudaGetLastError(), false;
-    for (int k = 0; k < P; k++) {
+    bool ok = cudaMemcpyAsync(b->d_toff, trail_offsets, (int64_t)(n_trails + 1) * 8, cudaMemcpyHostToDevice, cs) ==
+              cudaSuccess;
+    for (int k = 0; ok && k < P; k++) {
         const int32_t t0 = (int32_t)((int64_t)n_trails * k / P), t1 = (int32_t)((int64_t)n_trails * (k + 1) / P);
         const int64_t a = trail_offsets[t0], e = trail_offsets[t1];
-        if (e > a && cudaMemcpyAsync(b->d_trail + a, trail_lits + a, (e - a) * 4, cudaMemcpyHostToDevice, cs) !=
-                         cudaSuccess)
-            return cudaGetLastError(), false;
-        if (cudaEventRecord(b->part_done[k], cs) != cudaSuccess || cudaStreamWaitEvent(0, b->part_done[k], 0) !=
-                                                                          cudaSuccess)
-            return cudaGetLastError(), false;
-        if (!apply_range(b, b->d_trail, b->d_toff, t0, t1, 0)) return false;
+        ok = (e <= a ||
+              cudaMemcpyAsync(b->d_trail + a, trail_lits + a, (e - a) * 4, cudaMemcpyHostToDevice, cs) ==
+                  cudaSuccess) &&
+             cudaEventRecord(b->part_done[k], cs) == cudaSuccess &&
+             cudaStreamWaitEvent(0, b->part_done[k], 0) == cudaSuccess &&
+             apply_range(b, b->d_trail, b->d_toff, t0, t1, 0);
     }
-    return true;
+    if (!ok) {
+        // the caller stages the trails again into the same buffers: no copy
+        // of this pass may still be in flight
+        cudaGetLastError();
+        cudaStreamSynchronize(cs);
+        cudaGetLastError();
+    }
+    return ok;
 }
 }  // namespace
 
@@ -871,8 +875,11 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
             rc = launch(b, b->d_trail, b->d_toff, n_trails, (int32_t *)dp[2], (int32_t *)dp[3], (int32_t *)dp[4],
                         (int64_t *)dp[5], (int32_t *)dp[6], (int32_t *)dp[7], counters ? (int64_t *)dp[8] : nullptr, 0,
                         applied);
-            if (rc != GPSAT_OK) return rc;
+            // also waits for the parts copied on the copy stream (the legacy
+            // stream waited for each), so no copy from the caller's buffers
+            // is left in flight even when the launch failed
             err = cudaStreamSynchronize(0);
+            if (rc != GPSAT_OK) return rc;
             if (err != cudaSuccess) return cuda_error(err, "bcp run");
             return GPSAT_OK;
         }
