@@ -24,6 +24,29 @@ def test_every_declared_symbol_is_exported(gpsat):
     assert not missing, f"declared but not exported: {missing}"
 
 
+def test_header_is_plain_c_and_links(gpsat, tmp_path):
+    """include/gpsat.h compiles as ISO C99 (no C++ types at the boundary), and a
+    C program that takes the address of every declared function links against
+    the library and runs (it only asks the version string)."""
+    import subprocess
+    names = declared_functions("gpsat.h")
+    src = tmp_path / "abi_c.c"
+    src.write_text("#include <stdio.h>\n#include \"gpsat.h\"\n"
+                   "typedef void (*fn)(void);\nstatic const fn table[] = {\n" + "".join(f"    (fn)&{n},\n" for n in names) +
+                   "};\n"
+                   "int main(void)\n{\n    printf(\"%s %d\\n\", gpsat_version(), (int)(sizeof table / sizeof *table));\n"
+                   "    return 0;\n}\n")
+    exe = tmp_path / "abi_c"
+    lib = gpsat.LIB_PATH
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I", str(ROOT / "include"), str(src), "-o", str(exe), "-L", str(lib.parent),
+                        "-Wl,-rpath," + str(lib.parent), "-l" + lib.stem[3:]], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert "sm_103a" in out.stdout and out.stdout.split()[-1] == str(len(names))
+
+
 def test_version_and_errors(gpsat):
     assert "sm_103a" in gpsat.version()
     L = gpsat.lib()
