@@ -281,7 +281,7 @@ def ref_own_bcp_scaled(n=2000, trails=1024):
     """The reference's own BCP (its WatchedClausesList, host build) at a
     scaled-down size of the BCP workload: n=2000, m=8400, trails of 1-5% of
     the variables, one host core, one call per trail; the time is that of the
-    trail application alone (the driver times the assignments and the
+    trail application alone (ref_driver.cpp times the assignments and the
     new_decision calls, not the watch-list set-up before them)."""
     import oracle
     try:
