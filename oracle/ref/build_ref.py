@@ -21,7 +21,7 @@ Recipe (nothing in the reference tree is modified):
   3. link them with oracle/ref/ref_driver.cpp into a shared library.
 
 The reference checkout is named by $GPSAT_REFERENCE (the directory that holds
-its src/).  Without it (as on the GPU machine), an existing build-dir copy under
+its src/).  Without it (on a machine with no reference checkout), an existing build-dir copy under
 oracle/_ref/ is compiled instead; with neither, build() raises
 FileNotFoundError saying so.
 It needs Boost for nothing: the CLI/parser units that use Boost are skipped.
