@@ -539,6 +539,8 @@ class Batch:
             co = np.ascontiguousarray(jobs[1], np.int64)
             cl = np.ascontiguousarray(jobs[2], np.int32)
             nj = len(jf)
+            if len(co) != nj + 1 or (nj and (co[0] < 0 or (np.diff(co) < 0).any() or co[-1] > len(cl))):
+                raise GpsatError(-1, "cube_offsets must hold len(job_formula) + 1 non-decreasing offsets into cube_lits")
         check(lib().gpsat_batch_solve(self._h, ctypes.byref(o), _p(jf), _p(co), _p(cl), nj, _p(out["verdict"]),
                                       _p(out["model"]), _p(out["stats"]), _p(out["model_ok"]),
                                       _p(out["participation"])))

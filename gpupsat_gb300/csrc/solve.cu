@@ -410,10 +410,14 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
                                  int32_t *verdicts, int8_t *models, int64_t *stats, int32_t *model_ok,
                                  int32_t *participation)
 {
-    if (!b || !verdicts) return set_error(GPSAT_ERR_ARG, "gpsat_batch_solve: bad argument");
+    if (!b || !verdicts || n_jobs < 0) return set_error(GPSAT_ERR_ARG, "gpsat_batch_solve: bad argument");
     gpsat_solve_options o;
     if (opt) o = *opt;
     else gpsat_solve_options_default(&o);
+    if (o.log_participation < 0 || o.log_participation > 2)
+        return set_error(GPSAT_ERR_ARG, "log_participation must be 0, 1 or 2");
+    if (o.proof_words < 0) return set_error(GPSAT_ERR_ARG, "proof_words must be >= 0");
+    if (o.phase_init < 0 || o.phase_init > 2) return set_error(GPSAT_ERR_ARG, "phase_init must be 0, 1 or 2");
     cudaError_t err = cudaSetDevice(b->device);
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
     const int32_t F = b->n_formulas;
@@ -438,6 +442,8 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
             const int32_t f = job_formula[j];
             if (f < 0 || f >= F) return set_error(GPSAT_ERR_ARG, "job formula index out of range");
             const int64_t c0 = cube_offsets ? cube_offsets[j] : 0, c1 = cube_offsets ? cube_offsets[j + 1] : 0;
+            if (c0 < 0 || c1 < c0 || (c1 > c0 && !cube_lits))
+                return set_error(GPSAT_ERR_ARG, "bad cube offsets");
             for (int64_t k = c0; k < c1; k++) {
                 const int32_t d = cube_lits[k];
                 if (d == 0 || d > b->n_vars[f] || d < -b->n_vars[f])
@@ -472,11 +478,8 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
         b->cube_cap = (int64_t)cubes.size();
     }
     const int64_t V = b->var_off[F];
-    if (o.log_participation < 0 || o.log_participation > 2)
-        return set_error(GPSAT_ERR_ARG, "log_participation must be 0, 1 or 2");
     const int64_t PV = o.log_participation >= 2 ? 2 * V : V;
     // proof logs: proof_words per job
-    if (o.proof_words < 0) return set_error(GPSAT_ERR_ARG, "proof_words must be >= 0");
     b->proof_words = o.proof_words;
     if (o.proof_words > 0 && J > 0) {
         const int64_t need = (int64_t)J * o.proof_words * 4;
@@ -544,7 +547,6 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     P.o.learnt_inc = std::max(0, o.learnt_inc);
     P.o.minimize = o.minimize;
     P.o.conflict_budget = o.conflict_budget > 0 ? o.conflict_budget : INT64_MAX;
-    if (o.phase_init < 0 || o.phase_init > 2) return set_error(GPSAT_ERR_ARG, "phase_init must be 0, 1 or 2");
     P.o.phase_init = o.phase_init;
     P.o.log_participation = o.log_participation;
     P.o.check_every = 256;

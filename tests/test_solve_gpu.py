@@ -113,6 +113,35 @@ def test_conflict_budget_gives_unknown(gpsat, cuda_ok):
     assert out["stats"][0, 7] & 4
 
 
+def test_bad_jobs_and_options_are_refused(gpsat, cuda_ok):
+    """Cube offsets that do not index the cube literals, and out-of-range
+    options, are refused before anything runs; the batch still solves after."""
+    import ctypes
+    lits, off = gpsat.gen_random_ksat(78, 40, 170, 3)
+    b = gpsat.Batch([(lits, off)], [40])
+    jf = np.zeros(2, np.int32)
+    for co, cl in [(np.array([0, 1], np.int64), np.array([1], np.int32)),          # one offset short
+                   (np.array([0, 2, 1], np.int64), np.array([1, 2], np.int32)),    # going back
+                   (np.array([0, 1, 3], np.int64), np.array([1, 2], np.int32))]:   # past the literals
+        with pytest.raises(gpsat.GpsatError):
+            b.solve(jobs=(jf, co, cl))
+    # the library's own checks: offsets with no literal array, a negative offset
+    vp = ctypes.c_void_p
+    verdict = np.zeros(1, np.int32)
+    for co, cl in [(np.array([0, 1, 2], np.int64), None), (np.array([-1, 0, 0], np.int64), np.zeros(1, np.int32))]:
+        rc = gpsat.lib().gpsat_batch_solve(b._h, None, vp(jf.ctypes.data), vp(co.ctypes.data),
+                                           None if cl is None else vp(cl.ctypes.data), 2, vp(verdict.ctypes.data),
+                                           None, None, None, None)
+        assert rc == -1
+    for bad in (dict(phase_init=3), dict(proof_words=-1), dict(log_participation=5)):
+        with pytest.raises(gpsat.GpsatError):
+            b.solve(gpsat.solve_options(**bad))
+    out = b.solve(jobs=(jf, np.array([0, 1, 2], np.int64), np.array([1, -1], np.int32)))
+    assert out["verdict"][0] in (gpsat.SAT, gpsat.UNSAT)
+    assert out["verdict"][0] != gpsat.SAT or out["model_ok"][0] == 1
+    assert out["verdict"][0] == b.solve()["verdict"][0]
+
+
 def test_batched_workload_sample_matches_reference(gpsat, cuda_ok, solve_golden):
     """Instances of the batched-solve workload with n <= 150 (the first 160 of
     them), against the reference's own verdicts with its iteration cap lifted."""
