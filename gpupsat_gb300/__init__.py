@@ -368,6 +368,8 @@ class BCPBatch:
         trail_lits = np.ascontiguousarray(trail_lits, dtype=np.int32)
         trail_offsets = np.ascontiguousarray(trail_offsets, dtype=np.int64)
         T = len(trail_offsets) - 1
+        if T < 0 or (T > 0 and trail_offsets[-1] > len(trail_lits)):
+            raise ValueError("run_host: trail_offsets must have n_trails + 1 entries ending within trail_lits")
         if out is None:
             out = self.host_outputs(T, counters)
         else:

@@ -844,6 +844,11 @@ extern "C" int gpsat_bcp_run_host(gpsat_bcp *b, const int32_t *trail_lits, const
     if (err != cudaSuccess) return cuda_error(err, "cudaSetDevice");
     const int64_t nl = trail_offsets[n_trails];
     if (nl < 0 || (nl > 0 && !trail_lits)) return set_error(GPSAT_ERR_ARG, "bad trail offsets");
+    // every trail inside the nl literals that are copied in
+    if (trail_offsets[0] < 0) return set_error(GPSAT_ERR_ARG, "trail offsets must be >= 0");
+    for (int32_t t = 0; t < n_trails; t++)
+        if (trail_offsets[t + 1] < trail_offsets[t])
+            return set_error(GPSAT_ERR_ARG, "trail offsets must be non-decreasing");
     {
         // Every buffer page-locked (cudaHostAlloc / cudaHostRegister, as
         // torch's pin_memory): the trails are copied to the device by DMA

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "cdcl.cuh"
@@ -283,6 +284,18 @@ extern "C" int gpsat_batch_create(const int32_t *lits, const int64_t *clause_off
     if (!out || n_formulas <= 0 || !clause_offsets || !formula_offsets || !n_vars)
         return set_error(GPSAT_ERR_ARG, "gpsat_batch_create: bad argument");
     *out = nullptr;
+    // every offset, before any formula's clauses are read through them (the
+    // literals are checked as each formula is prepared)
+    if (formula_offsets[0] < 0) return set_error(GPSAT_ERR_FORMULA, "formula_offsets[0] must be >= 0");
+    for (int32_t f = 0; f < n_formulas; f++)
+        if (formula_offsets[f + 1] < formula_offsets[f])
+            return set_error(GPSAT_ERR_FORMULA, "formula offsets must be non-decreasing");
+    if (clause_offsets[formula_offsets[0]] < 0) return set_error(GPSAT_ERR_FORMULA, "clause offsets must be >= 0");
+    for (int64_t c = formula_offsets[0]; c < formula_offsets[n_formulas]; c++)
+        if (clause_offsets[c + 1] < clause_offsets[c])
+            return set_error(GPSAT_ERR_FORMULA, "clause offsets must be non-decreasing");
+    if (clause_offsets[formula_offsets[n_formulas]] > clause_offsets[formula_offsets[0]] && !lits)
+        return set_error(GPSAT_ERR_ARG, "null literal array");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -423,14 +436,17 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     const int32_t F = b->n_formulas;
     // jobs: given, or one per formula; preprocessing-decided formulas get none.
     // A job's level-0 facts are the literals preprocessing fixed, then its cube.
-    std::vector<int32_t> jinst, jcoff, jclen, cubes;
+    // (the previous solve's jobs are forgotten first: a call that fails
+    // leaves no proof log to read)
+    std::vector<int32_t> jinst, jcoff, jclen, cubes, caller_job;
     b->caller_job.clear();
+    b->job_verdict.clear();
     auto add_job = [&](int32_t f, const int32_t *cube, int64_t clen) {
         if (b->prep[f].verdict != GPSAT_UNKNOWN) {
-            b->caller_job.push_back(-1);
+            caller_job.push_back(-1);
             return;
         }
-        b->caller_job.push_back((int32_t)jinst.size());
+        caller_job.push_back((int32_t)jinst.size());
         jinst.push_back(f);
         jcoff.push_back((int32_t)cubes.size());
         for (int32_t l : b->prep[f].solved) cubes.push_back(l);
@@ -601,6 +617,7 @@ extern "C" int gpsat_batch_solve(gpsat_batch *b, const gpsat_solve_options *opt,
     err = cudaStreamSynchronize(st);
     if (err != cudaSuccess) return cuda_error(err, "solve");
     b->job_verdict = jv;
+    b->caller_job = std::move(caller_job);
     std::vector<int32_t> n_unsat(F, 0), n_jobs_f(F, 0);
     if (stats) std::memset(stats, 0, sizeof(int64_t) * (size_t)F * GPSAT_SOLVE_NSTATS);
     for (int32_t j = 0; j < J; j++) {

@@ -108,6 +108,9 @@ int gpsat_formula_export(const gpsat_formula *f, int32_t *lits, int64_t *offsets
  *   impl_lit[t*impl_cap ...]     (DIMACS) and
  *   impl_reason[t*impl_cap ...]  (index of the implying clause)
  *   counters[t*GPSAT_BCP_NCOUNTERS ...]  (may be NULL)
+ * Trail t is trail_lits[trail_offsets[t] .. trail_offsets[t+1]): the offsets
+ * must be non-decreasing from >= 0 (gpsat_bcp_run_host refuses others with
+ * GPSAT_ERR_ARG; the device entries read them as given).
  * Trails must not assign a variable both ways (GPSAT_BCP_BAD_TRAIL);
  * a variable repeated with the same sign is propagated twice, as in the
  * reference.  Clause length is limited to 2048 literals.                     */

@@ -69,6 +69,33 @@ def test_formula_validation(gpsat):
     assert f.info()["verdict"] == gpsat.UNSAT
 
 
+def test_batch_offsets_are_checked_before_anything_is_read(gpsat):
+    """gpsat_batch_create refuses offsets that go back, or literals that are
+    missing, before it reads a clause (and before it looks for a device)."""
+    vp = ctypes.c_void_p
+    L = gpsat.lib()
+
+    def create(lits, coff, foff, nv):
+        h = vp()
+        a = [None if x is None else vp(x.ctypes.data) for x in (lits, coff, foff, nv)]
+        return L.gpsat_batch_create(*a, len(nv), ctypes.byref(h)), h
+
+    lits = np.array([1, 2, -1, 2, 1, -2], np.int32)
+    nv = np.array([2, 2], np.int32)
+    for coff, foff in [(np.array([0, 2, 4, 6], np.int64), np.array([0, 2, 1], np.int64)),    # formulas going back
+                       (np.array([0, 4, 2, 6], np.int64), np.array([0, 2, 3], np.int64)),    # clauses going back
+                       (np.array([-2, 2, 4, 6], np.int64), np.array([0, 1, 3], np.int64))]:  # negative
+        rc, h = create(lits, coff, foff, nv)
+        assert rc == -4 and not h, L.gpsat_last_error()
+    rc, h = create(None, np.array([0, 2, 4, 6], np.int64), np.array([0, 1, 3], np.int64), nv)
+    assert rc == -1 and not h
+    # well-formed: past the checks (no device here, or a batch made and freed)
+    rc, h = create(lits, np.array([0, 2, 4, 6], np.int64), np.array([0, 1, 3], np.int64), nv)
+    assert rc in (0, -7), L.gpsat_last_error()
+    if rc == 0:
+        L.gpsat_batch_destroy(h)
+
+
 def test_preprocessing_decides_trivial_formulas(gpsat):
     assert gpsat.Formula.from_clauses([[1, -1], [2, -2, 3]]).info()["verdict"] == gpsat.SAT
     assert gpsat.Formula.from_clauses([[1], [-1], [1, 2]]).info()["verdict"] == gpsat.UNSAT

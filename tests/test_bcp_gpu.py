@@ -76,6 +76,21 @@ def test_bcp_edge_cases(gpsat, orc, cuda_ok):
     assert all(g["counters"][t, 5] == len(trails[t]) for t in ok)
 
 
+def test_bcp_bad_trail_offsets_are_refused(gpsat, cuda_ok):
+    """Host entry: offsets that go back, start below 0 or run past the literals
+    are refused before anything is copied; the handle still runs after."""
+    lits, off = gpsat.gen_random_ksat(9, 100, 426, 3)
+    b = gpsat.BCPBatch(gpsat.Formula(lits, off, 100), impl_cap=100)
+    tl = np.array([1, -2, 3, 4, -5, 6], np.int32)
+    for to in ([0, 4, 2, 6], [-1, 2, 6]):
+        with pytest.raises(gpsat.GpsatError):
+            b.run_host(tl, np.array(to, np.int64))
+    with pytest.raises(ValueError):
+        b.run_host(tl, np.array([0, 2, 9], np.int64))
+    g = b.run_host(tl, np.array([0, 2, 6], np.int64))
+    assert set(g["status"]) <= {0, 1}
+
+
 def test_bcp_slot_reuse_and_epoch_wrap(gpsat, orc, cuda_ok):
     # one slot serves 400 trails: it runs past its 255-trail epoch range and
     # wipes its list heads and clause states once

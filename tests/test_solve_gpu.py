@@ -133,6 +133,8 @@ def test_bad_jobs_and_options_are_refused(gpsat, cuda_ok):
                                            None if cl is None else vp(cl.ctypes.data), 2, vp(verdict.ctypes.data),
                                            None, None, None, None)
         assert rc == -1
+    with pytest.raises(gpsat.GpsatError):   # a refused solve leaves no jobs to read proofs of
+        b.proof(0)
     for bad in (dict(phase_init=3), dict(proof_words=-1), dict(log_participation=5)):
         with pytest.raises(gpsat.GpsatError):
             b.solve(gpsat.solve_options(**bad))
