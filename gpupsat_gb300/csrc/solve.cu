@@ -720,8 +720,11 @@ extern "C" int gpsat_batch_proof(const gpsat_batch *b, int32_t job, int32_t *ver
 extern "C" int gpsat_check_model(const int32_t *lits, const int64_t *offsets, int64_t n_clauses, const int8_t *model,
                                  int32_t n_vars, int64_t *first_false_clause)
 {
-    if (!offsets || !model || n_vars <= 0) return set_error(GPSAT_ERR_ARG, "gpsat_check_model: bad argument");
+    if (n_clauses < 0 || (n_clauses > 0 && (!offsets || !lits)) || !model || n_vars <= 0)
+        return set_error(GPSAT_ERR_ARG, "gpsat_check_model: bad argument");
     for (int64_t c = 0; c < n_clauses; c++) {
+        if (offsets[c + 1] < offsets[c] || offsets[c] < 0)
+            return set_error(GPSAT_ERR_FORMULA, "gpsat_check_model: offsets must be non-decreasing from >= 0");
         bool sat = false;
         for (int64_t k = offsets[c]; k < offsets[c + 1] && !sat; k++) {
             const int32_t d = lits[k];

@@ -145,6 +145,26 @@ def test_planted_generator(gpsat):
         gpsat.gen_planted(1, 50, 10, 3, 40, 0.9)   # communities of one variable cannot hold 3
 
 
+def test_host_model_checker(gpsat):
+    """gpsat_check_model: true for a satisfying model, false with the first
+    falsified clause otherwise; bad offsets and literals are errors."""
+    lits = np.array([1, 2, -1, 3, -2, -3], np.int32)
+    off = np.array([0, 2, 4, 6], np.int64)
+    assert gpsat.check_model(lits, off, np.array([1, -1, 1], np.int8), 3)
+    bad = ctypes.c_int64()
+    m = np.array([-1, -1, 1], np.int8)
+    L = gpsat.lib()
+    vp = ctypes.c_void_p
+    assert L.gpsat_check_model(vp(lits.ctypes.data), vp(off.ctypes.data), 3, vp(m.ctypes.data), 3,
+                               ctypes.byref(bad)) == 0 and bad.value == 0
+    good = np.array([1, -1, 1], np.int8)   # the scan reaches every clause
+    with pytest.raises(gpsat.GpsatError):
+        gpsat.check_model(lits, np.array([0, 4, 2, 6], np.int64), good, 3)    # offsets going back
+    with pytest.raises(gpsat.GpsatError):
+        gpsat.check_model(lits, off, good, 2)                                  # literal 3 out of range
+    assert L.gpsat_check_model(None, vp(off.ctypes.data), 3, vp(m.ctypes.data), 3, None) == -1
+
+
 def test_bcp_without_device_fails_loudly(gpsat):
     if gpsat.device_count() > 0:
         pytest.skip("a GPU is visible; covered by the GPU tests")
