@@ -102,8 +102,8 @@ __global__ void order_scatter(const int64_t *toff, int T, int64_t pivot, unsigne
 // (so the words need no clearing between launches: each launch writes them
 // all).  A literal out of range, or a variable given both signs, marks the
 // trail bad (the BCP kernel then reports GPSAT_BCP_BAD_TRAIL for it).
-constexpr int APPLY_NT = 512;
-constexpr int APPLY_CHUNK_WORDS = 16384;   // 64 KB: 262,144 variables per pass
+constexpr int APPLY_NT = 1024;
+constexpr int APPLY_CHUNK_WORDS = 32768;   // 128 KB: 524,288 variables per pass
 constexpr int64_t APPLY_MAX_BYTES = int64_t(8) << 30;   // above this the blocks assign their own trails
 
 // trails [t_begin, t_end) of the launch
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(APPLY_NT) apply_kernel(const int32_t *__restri
     }
 }
 
-// the 64 KB of dynamic shared memory needs the opt-in, once per device
+// the 128 KB of dynamic shared memory needs the opt-in, once per device
 cudaError_t apply_allow()
 {
     static std::atomic<unsigned long long> done{0};

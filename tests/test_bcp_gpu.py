@@ -33,9 +33,9 @@ def test_bcp_matches_reference_golden(gpsat, cuda_ok, bcp_golden):
     (20000, 4.2, 3, 512, 0.01, 0.05, 3),
     (500, 9.9, 4, 256, 0.05, 0.40, 4),
     (300, 21.0, 5, 256, 0.05, 0.50, 5),
-    # 262,150 variables: the trail-application kernel's second shared-memory
-    # chunk of assignment words holds one word (its variables 262,144 onward)
-    (262150, 4.2, 3, 48, 0.002, 0.01, 6),
+    # 524,300 variables: the trail-application kernel's second shared-memory
+    # chunk of assignment words holds one word (its variables 524,288 onward)
+    (524300, 4.2, 3, 32, 0.002, 0.01, 6),
 ])
 def test_bcp_matches_oracle_random(gpsat, orc, cuda_ok, n, ratio, k, T, fmin, fmax, seed):
     m = int(round(ratio * n))
