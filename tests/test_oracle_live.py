@@ -6,7 +6,8 @@ reference's own BCP (`WatchedClausesList::new_decision` driven as
 `ref_bcp`) and its full-scan evaluation (`ConflictAnalyzer::
 propagate_all_clauses`, `ref_scan`), compiled for the host from the
 reference's sources (oracle/ref/build_ref.py), beside the oracle on seeded
-formulas of clause widths 2 to 7 and ragged trails with the edge cases the
+formulas of clause widths 2 to 7, mixed widths up to 21 and long clauses of
+10 to 14 literals, with ragged trails that hold the edge cases the
 reference's trail application has: an empty trail, a repeated literal, a
 variable given both signs.  Skipped where the host build of the reference is
 not present."""
@@ -86,6 +87,55 @@ def make_trails(rng, n, T, fmax):
 # (k, n, clauses per variable, largest trail fraction)
 SHAPES = [(2, 40, 1.0, 0.5), (2, 300, 0.9, 0.1), (3, 60, 4.26, 0.5), (3, 600, 4.26, 0.2), (3, 1500, 3.5, 0.1),
           (4, 80, 9.9, 0.4), (5, 100, 21.0, 0.75), (7, 40, 60.0, 0.85)]
+
+
+def mixed_formula(seed, n, m, widths, bias):
+    """Clauses of the given widths on distinct variables; with bias > 0 a
+    literal is true under a hidden assignment only with probability bias and
+    the trails below follow that assignment, so long clauses also become unit
+    and conflicting."""
+    rng = np.random.default_rng(seed)
+    hidden = rng.random(n + 1) < 0.5
+    cls = []
+    for _ in range(m):
+        vs = rng.choice(np.arange(1, n + 1), size=int(rng.choice(widths)), replace=False)
+        pos = hidden[vs] == (rng.random(len(vs)) < bias) if bias > 0 else rng.random(len(vs)) < 0.5
+        cls.append(np.where(pos, vs, -vs))
+    off = np.zeros(m + 1, np.int64)
+    off[1:] = np.cumsum([len(c) for c in cls])
+    return np.concatenate(cls).astype(np.int32), off, hidden
+
+
+@pytest.mark.parametrize("strategy", ["watched", "full_scan"])
+@pytest.mark.parametrize("n,m,widths,bias,fmax", [(120, 400, (2, 2, 3, 3, 3, 4, 6, 9), 0.0, 0.1),
+                                                  (80, 400, tuple(range(10, 15)), 0.12, 0.9),
+                                                  (300, 900, (2, 3, 5, 8, 13, 21), 0.2, 0.3)])
+def test_oracle_matches_the_reference_on_mixed_widths(orc, ref, strategy, n, m, widths, bias, fmax):
+    seed = n + m
+    lits, off, hidden = mixed_formula(seed, n, m, widths, bias)
+    rng = np.random.default_rng(seed + 1)
+    tl, to = make_trails(rng, n, 12, fmax)
+    if bias:
+        # trails mostly follow the hidden assignment (4% of signs flipped)
+        v = np.abs(tl)
+        follow = hidden[v] != (rng.random(len(v)) < 0.04)
+        tl = np.where(follow, v, -v).astype(np.int32)
+        tl[to[2] + (to[3] - to[2]) - 1] = -tl[to[2]]        # keep trail 2's contradiction
+        tl[to[1] + (to[2] - to[1]) - 1] = tl[to[1]]         # and trail 1's repeat
+        tl[to[3]] = tl[to[3] + 1]                           # and trail 3's
+    cap = n + 8
+    r = ref_run(ref, lits, off, n, tl, to, cap, strategy)
+    o = orc.BCPOracle(lits, off, n).run(tl, to, impl_cap=cap, strategy=strategy)
+    assert r["status"][2] == -2 and r["n_impl"].sum() > 0 and (r["status"] == 1).any()
+    assert (r["status"] == 0).sum() > 1
+    for t in range(len(to) - 1):
+        kk = int(r["n_impl"][t])
+        assert (o["status"][t], o["conflict"][t], o["n_impl"][t]) == (r["status"][t], r["conflict"][t], kk), \
+            f"{widths} trail {t}"
+        assert np.array_equal(o["impl_lit"][t, :kk], r["impl_lit"][t, :kk]), f"{widths} trail {t}"
+        if strategy == "watched":
+            assert o["stop"][t] == r["stop"][t], f"{widths} trail {t}"
+            assert np.array_equal(o["impl_reason"][t, :kk], r["impl_reason"][t, :kk]), f"{widths} trail {t}"
 
 
 @pytest.mark.parametrize("strategy", ["watched", "full_scan"])
