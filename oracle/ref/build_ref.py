@@ -21,9 +21,10 @@ Recipe (nothing in the reference tree is modified):
   3. link them with oracle/ref/ref_driver.cpp into a shared library.
 
 The reference checkout is named by $GPSAT_REFERENCE (the directory that holds
-its src/).  Without it (on a machine with no reference checkout), an existing build-dir copy under
-oracle/_ref/ is compiled instead; with neither, build() raises
-FileNotFoundError saying so.
+its src/), else CHECKOUT below.  Without either (on a machine with no
+reference checkout), an existing build-dir copy under oracle/_ref/ is
+compiled instead; with none of them, build() raises FileNotFoundError saying
+so.
 It needs Boost for nothing: the CLI/parser units that use Boost are skipped.
 """
 from __future__ import annotations
@@ -60,12 +61,17 @@ HOST_SIDE = {"Utils/CUDAClauseVec.cu", "FileManager/FormulaData.cu", "Preprocess
 VARIANTS = {"stock": None, "nocap": ("#define MAX_ITERATIONS 1000", "#define MAX_ITERATIONS 2000000000")}
 
 
+# where this recipe reads the reference's sources when $GPSAT_REFERENCE is not
+# set: the read-only checkout of the container the library is developed in
+# (absent elsewhere, where the build-dir copy under oracle/_ref/ is used)
+CHECKOUT = Path("/root/reference")
+
+
 def reference_src() -> Path | None:
-    """src/ of the checkout named by $GPSAT_REFERENCE, or None."""
+    """src/ of the checkout named by $GPSAT_REFERENCE, else of CHECKOUT when
+    it is there, else None."""
     root = os.environ.get("GPSAT_REFERENCE")
-    if not root:
-        return None
-    cand = Path(root) / "src"
+    cand = Path(root) / "src" if root else CHECKOUT / "src"
     return cand if (cand / "SATSolver" / "SATSolver.cu").exists() else None
 
 
@@ -81,8 +87,8 @@ def _prepare_copy(variant: str) -> Path:
     ref = reference_src()
     if ref is None:
         if not (dst / "SATSolver" / "SATSolver.cu").exists():
-            raise FileNotFoundError("no build-dir copy of the reference under oracle/_ref and $GPSAT_REFERENCE "
-                                    "does not name a reference checkout (the directory holding src/)")
+            raise FileNotFoundError("no build-dir copy of the reference under oracle/_ref, and no reference "
+                                    f"checkout at $GPSAT_REFERENCE or {CHECKOUT} (the directory holding src/)")
         return dst
     stamp = dst / ".copied"
     if stamp.exists():
