@@ -10,6 +10,10 @@
 //                                        256-entry window and 8 trails in flight
 //                                        set on the way (the watched kernel's
 //                                        shape, which the full scan ignores)
+//   api_check config                    the solve options of the default
+//                                        SolverConfig, then of the reference's
+//                                        roles (last free variable, geometric
+//                                        restarts), then the library's defaults
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -18,8 +22,28 @@
 
 #include "gpsat.hpp"
 
+static void print_options(const gpsat_solve_options &o)
+{
+    std::printf("%d %d %d %.6g %.6g %d %d %d %lld %d %d\n", o.decide, o.restart, o.restart_base,
+                (double)o.restart_factor, (double)o.var_decay, o.learnt_first, o.learnt_inc, o.minimize,
+                (long long)o.conflict_budget, o.phase_init, o.max_slots);
+}
+
 int main(int argc, char **argv)
 {
+    if (argc == 2 && std::string(argv[1]) == "config") {
+        gpsat::SolverConfig c;
+        print_options(c.options());
+        gpsat::SolverConfig r;
+        r.decision = std::make_shared<gpsat::LastFreeVariable>();
+        r.restarts = std::make_shared<gpsat::GeometricRestarts>();
+        r.conflict_budget = 5000;
+        print_options(r.options());
+        gpsat_solve_options d;
+        if (gpsat_solve_options_default(&d) != GPSAT_OK) return 1;
+        print_options(d);
+        return 0;
+    }
     if (argc < 4) {
         std::fprintf(stderr, "usage: api_check rank|trails <cnf> <arg>\n");
         return 2;

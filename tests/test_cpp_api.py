@@ -69,6 +69,21 @@ def test_max_clause_chooser_ranks_like_the_reference(gpsat, api_check, tmp_path,
             assert v == int(order[i])
 
 
+def test_solver_roles_configure_the_options(api_check):
+    """The C++ roles of a default SolverConfig give the library's default
+    options, except the conflict budget: a SolverConfig solves to the end
+    unless given one, as the CLI does.  The reference's roles (last free
+    variable, geometric restarts) set its schedule: 100 conflicts, x1.3."""
+    r = subprocess.run([str(api_check), "config"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    default, parity, library = [row.split() for row in r.stdout.strip().split("\n")]
+    assert default[:8] + default[9:] == library[:8] + library[9:]
+    assert default[8] == "0" and int(library[8]) > 0
+    decide, restart, base, factor = int(parity[0]), int(parity[1]), int(parity[2]), float(parity[3])
+    assert (decide, restart, base) == (1, 2, 100) and abs(factor - 1.3) < 1e-6   # LAST_FREE, GEOMETRIC
+    assert int(parity[8]) == 5000 and parity[4:8] == library[4:8]
+
+
 def test_oracle_generator_matches_the_library(gpsat, orc):
     for seed, n, m, k in [(2024, 5000, 21000, 3), (5, 300, 2979, 5), (77, 60, 256, 4)]:
         a = orc.gen_random_ksat(seed, n, m, k)
